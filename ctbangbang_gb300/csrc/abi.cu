@@ -1,0 +1,494 @@
+// abi.cu -- the library's C ABI: context, device-resident stages, the
+// whole-scan device path and the drop-in module functions with the reference's
+// semantics (host buffers in, host buffers out, d_rebin handed from rebin_filter
+// to backproject).
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "adaptive_filter.h"
+#include "backproject.h"
+#include "ctbb_internal.h"
+#include "cuda_util.cuh"
+#include "finalize.h"
+#include "ramp_filter.h"
+#include "rebin.h"
+
+namespace ctbb {
+
+namespace {
+
+// Grow-only device buffer.
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need)
+    {
+        if (need <= bytes && ptr) return CTBB_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, need ? need : 16);
+        if (e != cudaSuccess) {
+            set_error("cudaMalloc of %zu bytes failed: %s", need, cudaGetErrorString(e));
+            ptr = nullptr;
+            return CTBB_ERR_ALLOC;
+        }
+        bytes = need;
+        return CTBB_OK;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+struct Context {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    std::atomic<uint64_t> launches{0};
+    // stage work buffers
+    DeviceBuffer raw_in, raw_filt, rebin, block, image, final_stack, scratch;
+    // tables
+    DeviceBuffer bp_views, bp_zpos, fin_offsets, fin_slices, fin_weights;
+    DeviceRebinTables rebin_tables;
+    RampFilterPlan ramp;
+    void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
+    int sms = 0;
+};
+
+Context &ctx()
+{
+    static Context *c = new Context;  // never destroyed: no CUDA calls at exit
+    return *c;
+}
+
+template <class T>
+int upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t s)
+{
+    CTBB_TRY(buf.ensure(v.size() * sizeof(T)));
+    if (!v.empty())
+        CTBB_CUDA_TRY(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return CTBB_OK;
+}
+
+int check_mr(const struct recon_metadata *mr)
+{
+    if (!mr) {
+        set_error("null recon_metadata");
+        return CTBB_ERR_ARGUMENT;
+    }
+    if (mr->ri.n_ffs == 0 || mr->ri.n_proj_pull == 0 || mr->cg.n_channels == 0 || mr->cg.n_rows == 0) {
+        set_error("recon_metadata is not planned (n_ffs / n_proj_pull / geometry unset)");
+        return CTBB_ERR_STATE;
+    }
+    return CTBB_OK;
+}
+
+// Default voxels-per-thread of the backprojector along z.
+constexpr int kBackprojectZpt = 8;
+
+int bp_zpt()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_ZPT");
+        int z = e ? atoi(e) : kBackprojectZpt;
+        return (z == 4 || z == 8 || z == 16 || z == 32) ? z : kBackprojectZpt;
+    }();
+    return v;
+}
+
+}  // namespace
+
+cudaStream_t current_stream() { return ctx().stream; }
+
+int num_sms()
+{
+    Context &c = ctx();
+    if (!c.sms) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        c.sms = n > 0 ? n : 1;
+    }
+    return c.sms;
+}
+
+void count_launch(uint64_t n) { ctx().launches += n; }
+
+int require_device()
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error("no CUDA device available (%s); this library has no CPU path",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        return CTBB_ERR_NO_DEVICE;
+    }
+    return CTBB_OK;
+}
+
+// ---- stage implementations (device pointers, stream-ordered) --------------
+
+static int do_adaptive(const struct recon_metadata &mr, const float *d_in, float *d_out)
+{
+    Context &c = ctx();
+    size_t n = adaptive_filter_scratch_floats(mr.ri.n_proj_pull);
+    CTBB_TRY(c.scratch.ensure(n * sizeof(float)));
+    return launch_adaptive_filter(mr, d_in, d_out, c.scratch.as<float>(), c.stream);
+}
+
+static int do_rebin(const struct recon_metadata &mr, const float *d_raw, float *d_rebin)
+{
+    Context &c = ctx();
+    RebinTables t;
+    CTBB_TRY(build_rebin_tables(mr, &t));
+    CTBB_TRY(upload_rebin_tables(t, &c.rebin_tables, c.stream));
+    return launch_rebin(t, c.rebin_tables, d_raw, d_rebin, c.stream);
+}
+
+static int do_filter(const struct recon_metadata &mr, float *d_rebin)
+{
+    Context &c = ctx();
+    BlockDims d = block_dims(mr);
+    std::vector<float> taps(2 * d.n_os);
+    CTBB_TRY(ctbb_load_filter(&mr, taps.data()));
+    CTBB_TRY(prepare_ramp_filter(taps.data(), (int)d.n_os, &c.ramp, c.stream));
+    return launch_ramp_filter(c.ramp, d_rebin, d.n_views * d.n_rows, c.stream);
+}
+
+static int do_backproject(const struct recon_metadata &mr, const float *d_rebin, float *d_block)
+{
+    Context &c = ctx();
+    BackprojectTables t;
+    CTBB_TRY(build_backproject_tables(mr, &t));
+    CTBB_TRY(upload(c.bp_views, t.views, c.stream));
+    CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_zpos.as<float>(), d_rebin, d_block,
+                              bp_zpt(), c.stream);
+}
+
+static int do_finalize(const struct recon_metadata &mr, const float *d_image, float *d_final, float mu_water)
+{
+    Context &c = ctx();
+    FinalizeTables t;
+    CTBB_TRY(build_finalize_tables(mr, &t));
+    CTBB_TRY(upload(c.fin_offsets, t.offsets, c.stream));
+    CTBB_TRY(upload(c.fin_slices, t.slices, c.stream));
+    CTBB_TRY(upload(c.fin_weights, t.weights, c.stream));
+    return launch_finalize(mr, t, c.fin_offsets.as<int>(), c.fin_slices.as<int>(), c.fin_weights.as<float>(),
+                           d_image, d_final, mu_water, c.stream);
+}
+
+}  // namespace ctbb
+
+using namespace ctbb;
+
+// --------------------------------------------------------------------------
+// misc
+// --------------------------------------------------------------------------
+
+extern "C" const char *ctbb_version(void) { return "ctbangbang_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" int ctbb_set_stream(void *stream)
+{
+    ctx().stream = reinterpret_cast<cudaStream_t>(stream);
+    return CTBB_OK;
+}
+
+extern "C" uint64_t ctbb_kernel_launch_count(void) { return ctx().launches.load(); }
+
+extern "C" int ctbb_release_workspace(void)
+{
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (DeviceBuffer *b : {&c.raw_in, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack, &c.scratch,
+                            &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices, &c.fin_weights})
+        b->release();
+    if (c.rebin_tables.base) cudaFree(c.rebin_tables.base);
+    c.rebin_tables = DeviceRebinTables{};
+    if (c.ramp.d_spectrum) cudaFree(c.ramp.d_spectrum);
+    c.ramp = RampFilterPlan{};
+    return CTBB_OK;
+}
+
+// sizeof(struct recon_metadata) and member offsets, in the order the tests use.
+extern "C" int ctbb_struct_layout(size_t *out, int n)
+{
+    size_t v[] = {
+        sizeof(struct recon_metadata),
+        offsetof(struct recon_metadata, flags), offsetof(struct recon_metadata, rp),
+        offsetof(struct recon_metadata, ri), offsetof(struct recon_metadata, cg),
+        offsetof(struct recon_metadata, ctd), offsetof(struct recon_metadata, tube_angles),
+        offsetof(struct recon_metadata, table_positions), offsetof(struct recon_params, nx),
+        offsetof(struct recon_params, table_dir), offsetof(struct recon_info, cb),
+        offsetof(struct ct_geom, table_direction),
+    };
+    int m = (int)(sizeof(v) / sizeof(v[0]));
+    for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
+    return m;
+}
+
+// --------------------------------------------------------------------------
+// device-resident stages
+// --------------------------------------------------------------------------
+
+extern "C" int ctbb_adaptive_filter_device(const struct recon_metadata *mr, const float *d_in, float *d_out)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    return do_adaptive(*mr, d_in, d_out);
+}
+
+extern "C" int ctbb_rebin_device(const struct recon_metadata *mr, const float *d_raw, float *d_rebin)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    return do_rebin(*mr, d_raw, d_rebin);
+}
+
+extern "C" int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os, const float *h_taps)
+{
+    clear_error();
+    if (!d_lines || !h_taps || n_os <= 0) {
+        set_error("ctbb_ramp_filter_device: bad argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    CTBB_TRY(prepare_ramp_filter(h_taps, n_os, &c.ramp, c.stream));
+    return launch_ramp_filter(c.ramp, d_lines, n_lines, c.stream);
+}
+
+extern "C" int ctbb_backproject_device(const struct recon_metadata *mr, const float *d_rebin, float *d_block)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    return do_backproject(*mr, d_rebin, d_block);
+}
+
+extern "C" int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image, float *d_final,
+                                    float mu_water)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    return do_finalize(*mr, d_image, d_final, mu_water);
+}
+
+extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
+{
+    if (check_mr(mr)) return 0;
+    BlockDims d = block_dims(*mr);
+    // raw window (copy) + filtered raw + rebin + image stack; pull windows of
+    // later blocks can be up to 128 frames longer than the planned first one.
+    size_t frame = d.n_rows_raw * d.n_channels;
+    size_t raw = (d.n_proj_pull + 256) * frame * sizeof(float);
+    size_t rebin = ((d.n_proj_pull + 256) / d.n_ffs) * d.n_rows * d.n_os * sizeof(float);
+    size_t image = (size_t)mr->rp.nx * mr->rp.ny * mr->ri.n_slices_recon * sizeof(float);
+    return 2 * raw + rebin + image;
+}
+
+extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+                                       float mu_water)
+{
+    clear_error();
+    if (!mr || !d_scan || !d_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_device: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+    const size_t n_readings = (size_t)mr->rp.n_readings;
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    const size_t n_block = mr->ri.n_slices_block;
+    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+    mr->ri.cb.block_idx = 0;
+    for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
+        struct recon_info ri;
+        CTBB_TRY(plan_next_block(*mr, &ri));
+        mr->ri = ri;
+        BlockDims d = block_dims(*mr);
+        // the block's pull window: a view into the resident scan when it lies
+        // inside the data, else a zero-filled copy (frames past either end read 0)
+        long long s0 = (long long)(int)mr->ri.idx_pull_start;
+        long long s1 = s0 + (long long)d.n_proj_pull;
+        const float *d_win = nullptr;
+        if (s0 >= 0 && s1 <= (long long)n_readings) {
+            d_win = d_scan + (size_t)s0 * frame;
+        } else {
+            CTBB_TRY(c.raw_in.ensure(d.raw_elems() * sizeof(float)));
+            CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, d.raw_elems() * sizeof(float), c.stream));
+            long long a = s0 < 0 ? 0 : s0, e = s1 > (long long)n_readings ? (long long)n_readings : s1;
+            if (e > a)
+                CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - s0) * frame,
+                                              d_scan + (size_t)a * frame, (size_t)(e - a) * frame * sizeof(float),
+                                              cudaMemcpyDeviceToDevice, c.stream));
+            d_win = c.raw_in.as<float>();
+        }
+        CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
+        CTBB_TRY(do_adaptive(*mr, d_win, c.raw_filt.as<float>()));
+        CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
+        CTBB_TRY(do_rebin(*mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+        CTBB_TRY(do_filter(*mr, c.rebin.as<float>()));
+        float *slab = c.image.as<float>() + b * n_block * plane;
+        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>(), slab));
+    }
+    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), d_final, mu_water));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
+// --------------------------------------------------------------------------
+// drop-in module functions (host buffers)
+// --------------------------------------------------------------------------
+
+extern "C" int ctbb_adaptive_filter_kk(struct recon_metadata *mr)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    if (!mr->ctd.raw) {
+        set_error("adaptive_filter_kk: ctd.raw is null");
+        return CTBB_ERR_STATE;
+    }
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    BlockDims d = block_dims(*mr);
+    size_t bytes = d.raw_elems() * sizeof(float);
+    CTBB_TRY(c.raw_in.ensure(bytes));
+    CTBB_TRY(c.raw_filt.ensure(bytes));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.ptr, mr->ctd.raw, bytes, cudaMemcpyHostToDevice, c.stream));
+    CTBB_TRY(do_adaptive(*mr, c.raw_in.as<float>(), c.raw_filt.as<float>()));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.raw, c.raw_filt.ptr, bytes, cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_rebin_filter(struct recon_metadata *mr)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    if (!mr->ctd.raw) {
+        set_error("rebin_filter: ctd.raw is null");
+        return CTBB_ERR_STATE;
+    }
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    BlockDims d = block_dims(*mr);
+    size_t raw_bytes = d.raw_elems() * sizeof(float);
+    size_t rebin_bytes = d.rebin_elems() * sizeof(float);
+    CTBB_TRY(c.raw_in.ensure(raw_bytes));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.ptr, mr->ctd.raw, raw_bytes, cudaMemcpyHostToDevice, c.stream));
+    // d_rebin belongs to the caller until backproject frees it (src/backproject.cu:99);
+    // a buffer this library handed out and nobody consumed is released first.
+    if (mr->ctd.d_rebin && mr->ctd.d_rebin == c.our_d_rebin) cudaFree(mr->ctd.d_rebin);
+    mr->ctd.d_rebin = nullptr;
+    float *d_rebin = nullptr;
+    CTBB_CUDA_TRY(cudaMalloc(&d_rebin, rebin_bytes));
+    mr->ctd.d_rebin = d_rebin;
+    c.our_d_rebin = d_rebin;
+    CTBB_TRY(do_rebin(*mr, c.raw_in.as<float>(), d_rebin));
+    CTBB_TRY(do_filter(*mr, d_rebin));
+    if (mr->flags.testing && mr->ctd.rebin)
+        CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.rebin, d_rebin, rebin_bytes, cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_backproject(struct recon_metadata *mr)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    if (!mr->ctd.d_rebin || !mr->ctd.image) {
+        set_error("backproject: ctd.d_rebin (from rebin_filter) or ctd.image is null");
+        return CTBB_ERR_STATE;
+    }
+    if (mr->ri.cb.block_idx < 1 || (size_t)mr->ri.cb.block_idx > mr->ri.n_blocks) {
+        set_error("backproject: block_idx %d outside 1..%zu", mr->ri.cb.block_idx, mr->ri.n_blocks);
+        return CTBB_ERR_STATE;
+    }
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    size_t block_elems = plane * mr->ri.n_slices_block;
+    CTBB_TRY(c.block.ensure(block_elems * sizeof(float)));
+    CTBB_TRY(do_backproject(*mr, mr->ctd.d_rebin, c.block.as<float>()));
+    size_t block_offset = (size_t)(mr->ri.cb.block_idx - 1) * block_elems;
+    CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.image + block_offset, c.block.ptr, block_elems * sizeof(float),
+                                  cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    CTBB_CUDA_TRY(cudaFree(mr->ctd.d_rebin));
+    if (c.our_d_rebin == mr->ctd.d_rebin) c.our_d_rebin = nullptr;
+    mr->ctd.d_rebin = nullptr;
+    return CTBB_OK;
+}
+
+static int finalize_common(struct recon_metadata *mr, float mu_water)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    if (!mr->ctd.image) {
+        set_error("finalize_image_stack: ctd.image is null");
+        return CTBB_ERR_STATE;
+    }
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    size_t n_img = plane * mr->ri.n_slices_recon;
+    int n_final = ctbb_n_slices_final(mr);
+    size_t n_out = plane * (size_t)(n_final > 0 ? n_final : 0);
+    CTBB_TRY(c.image.ensure(n_img * sizeof(float)));
+    CTBB_TRY(c.final_stack.ensure(n_out * sizeof(float)));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(c.image.ptr, mr->ctd.image, n_img * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    float *host = (float *)calloc(n_out ? n_out : 1, sizeof(float));
+    if (!host) {
+        set_error("finalize_image_stack: host allocation failed");
+        return CTBB_ERR_ALLOC;
+    }
+    CTBB_CUDA_TRY(cudaMemcpyAsync(host, c.final_stack.ptr, n_out * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    mr->ctd.final_image_stack = host;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_finalize_image_stack(struct recon_metadata *mr) { return finalize_common(mr, 0.0f); }
+
+extern "C" int ctbb_finalize_image_stack_hu(struct recon_metadata *mr, float mu_water)
+{
+    if (!(mu_water > 0.0f)) {
+        set_error("finalize_image_stack_hu: mu_water must be > 0");
+        return CTBB_ERR_ARGUMENT;
+    }
+    return finalize_common(mr, mu_water);
+}
+
+// C++-linkage drop-ins with the reference module signatures.
+int adaptive_filter_kk(struct recon_metadata *mr) { return ctbb_adaptive_filter_kk(mr); }
+int rebin_filter(struct recon_metadata *mr) { return ctbb_rebin_filter(mr); }
+int backproject(struct recon_metadata *mr) { return ctbb_backproject(mr); }
+int finalize_image_stack(struct recon_metadata *mr) { return ctbb_finalize_image_stack(mr); }

@@ -1,0 +1,263 @@
+// adaptive_filter.cu -- Kachelriess-Kalender adaptive raw-data filter.
+//
+// Reference: adaptive_filter_kk (src/preprocessing.cu:31-156) and its kernels
+// (include/preprocessing.cuh:32-285), the reference's only implementation (it
+// has no CPU twin; src/main.cu:222 runs it on every block).  Per pull window of
+// P frames:
+//   1. sup[p]      = max(0, max of frame p)                        (extract_sup)
+//   2. smooth[p]   = mean of sup over an 18 deg window, clamped     (smooth_sup)
+//   3. ecc[p]      = clamp(((1 - min/max) - 0.3) / 0.2, 0, 1) over a
+//                    180 deg window of smooth; min/max kept         (eccentricity)
+//   4. T[p]        = <= 20-step bisection between min and max so that the
+//                    fraction of the 180 deg window of smooth above T matches
+//                    F_MAX * strength * ecc within 1 %                (find_thresholds)
+//   5. out         = 5x5x5 normalised triangle smoothing of samples > T[p],
+//                    other samples copied                          (filter_projections)
+// With strength 0 the stopping test divides by zero and T climbs toward the
+// window maximum; samples above it are still smoothed.  That behaviour is kept.
+//
+// Every float operation is written as a separate rounding (__f*_rn) in the
+// reference's order, so the result equals the reference kernels evaluated
+// without fused multiply-adds.  GB300 mapping: step 1 is a CTA reduction per
+// frame, steps 2-3 one thread per frame, step 4 one warp per frame (the window
+// counts are integers, so splitting them across lanes is exact), step 5 a
+// shared-memory tiled stencil.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "adaptive_filter.h"
+#include "ctbb_internal.h"
+#include "cuda_util.cuh"
+
+namespace ctbb {
+
+namespace {
+
+constexpr float kFMax = 0.03f;  // F_MAX, include/preprocessing.cuh:23
+constexpr float kPiAf = kPiBackproject;
+
+// triangle_3d(5, i, j, k) = (3-|i-3|) + (3-|j-3|) + (3-|k-3|) + 1
+// (include/preprocessing.cuh:64-67); its peak is at index 3 of 0..4.
+__host__ __device__ constexpr int tri1(int i) { return 3 - (i > 3 ? i - 3 : 3 - i); }
+
+struct AfParams {
+    const float *raw;
+    float *out;
+    float *sup, *smooth, *ecc, *pmax, *pmin, *thr;
+    int P, R, N;
+    int n_proj_ffs;
+    int n_avg, avg_offset;
+    int n_range, range_offset;
+    float strength;
+};
+
+__global__ void af_sup_kernel(AfParams p)
+{
+    int proj = blockIdx.x;
+    size_t frame = (size_t)p.R * p.N;
+    const float *src = p.raw + (size_t)proj * frame;
+    float m = 0.0f;
+    for (size_t i = threadIdx.x; i < frame; i += blockDim.x) m = fmaxf(m, src[i]);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) p.sup[proj] = m;
+    }
+}
+
+__global__ void af_smooth_kernel(AfParams p)
+{
+    int proj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (proj >= p.P) return;
+    float w = __fdiv_rn(1.0f, (float)p.n_avg);
+    float acc = 0.0f;
+    int max_idx = p.P - 1;
+    for (int i = 0; i < p.n_avg; i++) {
+        int idx = proj - p.avg_offset + i;
+        idx = idx < 0 ? 0 : (idx > max_idx ? max_idx : idx);
+        acc = __fadd_rn(acc, __fmul_rn(w, p.sup[idx]));
+    }
+    p.smooth[proj] = acc;
+}
+
+__global__ void af_ecc_kernel(AfParams p)
+{
+    int proj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (proj >= p.P) return;
+    int max_idx = p.P - 1;
+    float vmax = 0.0f, vmin = 10000.0f;
+    for (int i = 0; i < p.n_range; i++) {
+        int idx = proj - p.range_offset + i;
+        idx = idx < 0 ? 0 : (idx > max_idx ? max_idx : idx);
+        float v = p.smooth[idx];
+        if (v > vmax) vmax = v;
+        if (v < vmin) vmin = v;
+    }
+    p.pmax[proj] = vmax;
+    p.pmin[proj] = vmin;
+    float e = __fsub_rn(1.0f, __fdiv_rn(vmin, vmax));
+    e = __fdiv_rn(__fsub_rn(e, 0.3f), __fsub_rn(0.5f, 0.3f));
+    float out;
+    if (e > 1) out = 1.0f;
+    else if (e < 0) out = 0.0f;
+    else out = e;
+    p.ecc[proj] = out;
+}
+
+// rhs() of include/preprocessing.cuh:32-62, the window count split over a warp.
+__device__ float window_fraction(const AfParams &p, int start_idx, float T, int lane)
+{
+    int numel = p.n_range;
+    int max_idx = p.P - 1;
+    int diff = start_idx + (numel - 1);
+    if (diff < (numel - 1)) {
+        numel += start_idx;
+        start_idx = 0;
+    }
+    if (diff > max_idx) numel -= (diff - max_idx);
+    int count = 0;
+    for (int i = lane; i < numel; i += 32) count += (p.smooth[start_idx + i] > T) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+    const float inv_pi = 1.0f / kPiAf;
+    return __fmul_rn(__fmul_rn(inv_pi, (float)count), __fdiv_rn(1.0f, (float)p.n_proj_ffs));
+}
+
+__global__ void af_threshold_kernel(AfParams p)
+{
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= p.P) return;
+    int proj = warp;
+    float lower = p.pmin[proj];
+    float upper = p.pmax[proj];
+    float T = __fdiv_rn(__fadd_rn(p.pmax[proj], p.pmin[proj]), 2.0f);
+    float lhs = __fmul_rn(__fmul_rn(kFMax, p.strength), p.ecc[proj]);
+    int start = proj - p.range_offset;
+    float rhs = window_fraction(p, start, T, lane);
+    int iter = 0;
+    // (|lhs - rhs| / lhs) > 0.01 with the float quotient promoted to double
+    while ((double)__fdiv_rn(fabsf(__fsub_rn(lhs, rhs)), lhs) > 0.01) {
+        if (iter >= 20) break;
+        iter += 1;
+        if (rhs > lhs) lower = T;
+        else if (rhs < lhs) upper = T;
+        else break;
+        T = __fdiv_rn(__fadd_rn(lower, upper), 2.0f);
+        rhs = window_fraction(p, start, T, lane);
+    }
+    if (lane == 0) p.thr[proj] = T;
+}
+
+// Stencil tile: TP frames x TR rows x TC channels of output per CTA.
+constexpr int TP = 4, TR = 8, TC = 32;
+constexpr int SP = TP + 4, SR = TR + 4, SC = TC + 4;
+
+__constant__ float c_tri[125];  // weight of tap (ii, jj, kk) at [ii][jj][kk]
+
+__global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
+{
+    __shared__ float tile[SP][SR][SC];
+    int c0 = blockIdx.x * TC, r0 = blockIdx.y * TR, p0 = blockIdx.z * TP;
+    size_t frame = (size_t)p.R * p.N;
+    for (int t = threadIdx.x; t < SP * SR * SC; t += blockDim.x) {
+        int sc = t % SC, sr = (t / SC) % SR, sp = t / (SC * SR);
+        int gc = c0 + sc - 2, gr = r0 + sr - 2, gp = p0 + sp - 2;
+        float v = 0.0f;
+        if (gc >= 0 && gc < p.N && gr >= 0 && gr < p.R && gp >= 0 && gp < p.P)
+            v = __ldg(p.raw + (size_t)gp * frame + (size_t)gr * p.N + gc);
+        tile[sp][sr][sc] = v;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < TP * TR * TC; t += blockDim.x) {
+        int lc = t % TC, lr = (t / TC) % TR, lp = t / (TC * TR);
+        int gc = c0 + lc, gr = r0 + lr, gp = p0 + lp;
+        if (gc >= p.N || gr >= p.R || gp >= p.P) continue;
+        float x = tile[lp + 2][lr + 2][lc + 2];
+        float T = p.thr[gp];
+        float y = x;
+        if (x > T) {
+            // norm = sum of in-bounds weights: an exact integer, independent of order
+            int ni = 0, nj = 0, nk = 0, si = 0, sj = 0, sk = 0;
+            for (int d = 0; d < 5; ++d) {
+                if (gc + d - 2 >= 0 && gc + d - 2 < p.N) { ni++; si += tri1(d); }
+                if (gr + d - 2 >= 0 && gr + d - 2 < p.R) { nj++; sj += tri1(d); }
+                if (gp + d - 2 >= 0 && gp + d - 2 < p.P) { nk++; sk += tri1(d); }
+            }
+            float norm = (float)(nj * nk * si + ni * nk * sj + ni * nj * sk + ni * nj * nk);
+            float val = 0.0f;
+            for (int ii = 0; ii < 5; ii++)
+                for (int jj = 0; jj < 5; jj++)
+#pragma unroll
+                    for (int kk = 0; kk < 5; kk++)
+                        val = __fadd_rn(val, __fmul_rn(tile[lp + kk][lr + jj][lc + ii], c_tri[ii * 25 + jj * 5 + kk]));
+            y = __fmul_rn(__fdiv_rn(1.0f, norm), val);
+        }
+        p.out[(size_t)gp * frame + (size_t)gr * p.N + gc] = y;
+    }
+}
+
+}  // namespace
+
+size_t adaptive_filter_scratch_floats(size_t n_proj_pull) { return 6 * n_proj_pull; }
+
+int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                           float *d_scratch, cudaStream_t stream)
+{
+    static bool tri_uploaded = false;
+    if (!tri_uploaded) {
+        float tri[125];
+        for (int ii = 0; ii < 5; ii++)
+            for (int jj = 0; jj < 5; jj++)
+                for (int kk = 0; kk < 5; kk++)
+                    tri[ii * 25 + jj * 5 + kk] = (float)(tri1(ii) + tri1(jj) + tri1(kk) + 1);
+        CTBB_CUDA_TRY(cudaMemcpyToSymbol(c_tri, tri, sizeof(tri)));
+        tri_uploaded = true;
+    }
+    AfParams p;
+    p.raw = d_in;
+    p.out = d_out;
+    p.P = (int)mr.ri.n_proj_pull;
+    p.R = (int)mr.cg.n_rows_raw;
+    p.N = (int)mr.cg.n_channels;
+    p.n_proj_ffs = (int)mr.cg.n_proj_ffs;
+    p.sup = d_scratch;
+    p.smooth = d_scratch + p.P;
+    p.ecc = d_scratch + 2 * (size_t)p.P;
+    p.pmax = d_scratch + 3 * (size_t)p.P;
+    p.pmin = d_scratch + 4 * (size_t)p.P;
+    p.thr = d_scratch + 5 * (size_t)p.P;
+    // window sizes, include/preprocessing.cuh:92-96 and :119-122
+    int n_avg = (int)ceilf((18.0f / 360.0f) * (float)p.n_proj_ffs);
+    n_avg = n_avg + (1 - n_avg % 2);
+    p.n_avg = n_avg;
+    p.avg_offset = (int)floorf((float)(n_avg / 2));
+    int n_range = (int)ceilf((180.0f / 360.0f) * (float)p.n_proj_ffs);
+    n_range = n_range + (1 - n_range % 2);
+    p.n_range = n_range;
+    p.range_offset = (int)floorf((float)(n_range / 2));
+    p.strength = mr.rp.adaptive_filtration_s;
+    if (p.P <= 0 || p.R <= 0 || p.N <= 0) {
+        set_error("adaptive filter: empty pull window");
+        return CTBB_ERR_ARGUMENT;
+    }
+    af_sup_kernel<<<p.P, 256, 0, stream>>>(p);
+    af_smooth_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
+    af_ecc_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
+    af_threshold_kernel<<<(p.P * 32 + 255) / 256, 256, 0, stream>>>(p);
+    dim3 grid((p.N + TC - 1) / TC, (p.R + TR - 1) / TR, (p.P + TP - 1) / TP);
+    if (grid.z > 65535) {
+        set_error("adaptive filter: %d frames exceed the launch grid", p.P);
+        return CTBB_ERR_ARGUMENT;
+    }
+    af_filter_kernel<<<grid, 256, 0, stream>>>(p);
+    count_launch(5);
+    CTBB_CUDA_TRY(cudaGetLastError());
+    return CTBB_OK;
+}
+
+}  // namespace ctbb

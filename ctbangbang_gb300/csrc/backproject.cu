@@ -1,0 +1,227 @@
+// backproject.cu -- weighted-FBP cone-beam backprojection of one 32-slice block.
+//
+// Algorithm of the reference CPU backprojector (src/backproject_cpu.cu:49-154),
+// the path this library must match:
+//
+//   for each half-turn angle i < n_proj_turn/2 and voxel (x, y, z):
+//     s = sum_k interp2(view(i + k n/2); p_idx, q_idx) * W(q),  h = sum_k W(q)
+//     image += (s / h) * 2 pi' / n_proj_turn   (if h != 0)
+//   theta = tube_start + 2 pi' i / n_proj_turn + k pi',  p = x sin - y cos,
+//   p_idx = p / (r_f fai / 2) + 2 cc,  ray = z_rot (theta - asin(p / r_f)) / (2 pi'),
+//   l = sqrt(r_f^2 - p^2) - x cos - y sin,  q = (z - ray) / (l tan(theta_cone / 2)),
+//   q_idx = (q + 1)/2 (R - 1) + k R,  W(q) = 1 (|q| < 0.6), cos^2 taper to |q| = 1.
+//
+// interp2 (src/interp.cu:29-64) returns 0 when p_idx or q_idx leaves
+// [0, dim - 2]; the weight W is still added to h in that case, and this kernel
+// keeps that rule.  The reference's pi' = 3.1415368979f is used where it uses it.
+//
+// GB300 mapping: one thread per (x, y) column and ZPT consecutive slices; the
+// per-(x, y, view) geometry (asin, sqrt, reciprocal) is computed once and
+// amortised over the z-column held in registers (s, h, image per slice).  The
+// per-view trigonometric table is built on the host with the reference's float
+// expressions.  Samples are gathered through the read-only cache.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "backproject.h"
+#include "ctbb_internal.h"
+#include "cuda_util.cuh"
+
+namespace ctbb {
+
+namespace {
+
+struct BpParams {
+    const float *rebin;    // [V][R][Nos]
+    float *out;            // [n_slices_block][ny][nx]
+    const float4 *views;   // [n_half][nht] {theta, sin, cos, 0}
+    const float *zpos;     // [n_slices_block]
+    int nx, ny, n_slices, nos, n_rows, nht, n_half;
+    float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
+    float inv_ds_half;     // 1 / (r_f fai / 2)
+    float two_cc;          // 2 * central channel
+    float inv_rf, rf2;
+    float zrot_over_2pi;
+    float tan_cone;
+    float half_rows;       // (R - 1) / 2
+    float taper_scale;     // (pi'/2) / (1 - Q)
+    float out_scale;       // 2 pi' / n_proj_turn
+};
+
+constexpr float kQ = 0.6f;
+
+template <int ZPT>
+__global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
+{
+    int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    int z0 = blockIdx.z * ZPT;
+    if (xi >= p.nx || yi >= p.ny) return;
+    float x = p.pix_x * ((float)xi - p.x_c) + p.x0;
+    float y = p.pix_y * ((float)yi - p.y_c) + p.y0;
+
+    float zp[ZPT], img[ZPT];
+#pragma unroll
+    for (int z = 0; z < ZPT; ++z) {
+        zp[z] = (z0 + z < p.n_slices) ? __ldg(p.zpos + z0 + z) : 0.0f;
+        img[z] = 0.0f;
+    }
+    const size_t view_stride = (size_t)p.n_rows * p.nos;
+    const float p_max = (float)(p.nos - 2);
+    const float q_max_last = (float)(p.n_rows - 2);
+
+    for (int i = 0; i < p.n_half; ++i) {
+        float s[ZPT], h[ZPT];
+#pragma unroll
+        for (int z = 0; z < ZPT; ++z) {
+            s[z] = 0.0f;
+            h[z] = 0.0f;
+        }
+        for (int k = 0; k < p.nht; ++k) {
+            float4 t = __ldg(p.views + (size_t)i * p.nht + k);
+            float phat = x * t.y - y * t.z;
+            float p_idx = phat * p.inv_ds_half + p.two_cc;
+            bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
+            float ray = (t.x - asinf(phat * p.inv_rf)) * p.zrot_over_2pi;
+            float lhat = sqrtf(p.rf2 - phat * phat) - x * t.z - y * t.y;
+            float inv_den = 1.0f / (lhat * p.tan_cone);
+            float q_off = -ray * inv_den;
+            float q_lim = (k == p.nht - 1) ? q_max_last : 3.0e38f;
+            int ip = p_ok ? (int)p_idx : 0;
+            float wp = p_idx - (float)ip;
+            const float *view = p.rebin + ((size_t)i + (size_t)k * p.n_half) * view_stride + ip;
+#pragma unroll
+            for (int z = 0; z < ZPT; ++z) {
+                float q = fmaf(zp[z], inv_den, q_off);
+                float aq = fabsf(q);
+                if (aq < 1.0f) {
+                    float w = 1.0f;
+                    if (aq >= kQ) {
+                        float c = __cosf((aq - kQ) * p.taper_scale);
+                        w = c * c;
+                    }
+                    h[z] += w;
+                    float ql = (q + 1.0f) * p.half_rows;
+                    if (p_ok && ql <= q_lim) {
+                        int iq = (int)ql;
+                        float wq = ql - (float)iq;
+                        const float *r0 = view + (size_t)iq * p.nos;
+                        float v00 = __ldg(r0), v01 = __ldg(r0 + 1);
+                        float v10 = __ldg(r0 + p.nos), v11 = __ldg(r0 + p.nos + 1);
+                        float c0 = fmaf(wp, v01 - v00, v00);
+                        float c1 = fmaf(wp, v11 - v10, v10);
+                        s[z] = fmaf(w, fmaf(wq, c1 - c0, c0), s[z]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int z = 0; z < ZPT; ++z)
+            if (h[z] != 0.0f) img[z] += s[z] / h[z];
+    }
+    size_t plane = (size_t)p.nx * p.ny;
+#pragma unroll
+    for (int z = 0; z < ZPT; ++z)
+        if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z] * p.out_scale;
+}
+
+}  // namespace
+
+int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables *t)
+{
+    const struct ct_geom &cg = mr.cg;
+    const struct recon_params &rp = mr.rp;
+    const float pi = kPiBackproject;
+    BlockDims d = block_dims(mr);
+    if (d.n_half_turns <= 0) {
+        set_error("backproject: pull window holds no complete half turn");
+        return CTBB_ERR_STATE;
+    }
+    t->tube_start = bp_tube_start(mr);
+    t->nht = d.n_half_turns;
+    t->n_half = (int)(cg.n_proj_turn / 2);
+    t->n_slices = (int)mr.ri.n_slices_block;
+    t->views.resize((size_t)t->n_half * t->nht * 4);
+    for (int i = 0; i < t->n_half; ++i)
+        for (int k = 0; k < t->nht; ++k) {
+            // src/backproject_cpu.cu:102-103
+            float theta = t->tube_start + (2.0f * pi / (float)cg.n_proj_turn) * (float)i + (float)k * pi;
+            float *v = &t->views[((size_t)i * t->nht + k) * 4];
+            v[0] = theta;
+            v[1] = std::sin(theta);
+            v[2] = std::cos(theta);
+            v[3] = 0.0f;
+        }
+    t->zpos.resize(t->n_slices);
+    for (int zi = 0; zi < t->n_slices; ++zi)  // src/backproject_cpu.cu:107
+        t->zpos[zi] = (float)zi * rp.coll_slicewidth + cg.z_rot / 2.0f +
+                      cg.z_rot * t->tube_start / (2.0f * pi);
+    return CTBB_OK;
+}
+
+int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
+                       const float4 *d_views, const float *d_zpos, const float *d_rebin,
+                       float *d_block, int zpt, cudaStream_t stream)
+{
+    const struct ct_geom &cg = mr.cg;
+    const struct recon_params &rp = mr.rp;
+    const float pi = kPiBackproject;
+    BpParams p;
+    p.rebin = d_rebin;
+    p.out = d_block;
+    p.views = d_views;
+    p.zpos = d_zpos;
+    p.nx = (int)rp.nx;
+    p.ny = (int)rp.ny;
+    p.n_slices = t.n_slices;
+    p.nos = (int)cg.n_channels_oversampled;
+    p.n_rows = (int)cg.n_rows;
+    p.nht = t.nht;
+    p.n_half = t.n_half;
+    p.pix_x = rp.recon_fov / (float)rp.nx;
+    p.pix_y = rp.recon_fov / (float)rp.ny;
+    p.x_c = (float)(rp.nx - 1) / 2.0f;
+    p.y_c = (float)(rp.ny - 1) / 2.0f;
+    p.x0 = rp.x_origin;
+    p.y0 = rp.y_origin;
+    p.inv_ds_half = 1.0f / (cg.r_f * cg.fan_angle_increment / 2.0f);
+    p.two_cc = 2.0f * cg.central_channel;
+    p.inv_rf = 1.0f / cg.r_f;
+    p.rf2 = cg.r_f * cg.r_f;
+    p.zrot_over_2pi = cg.z_rot / (2.0f * pi);
+    p.tan_cone = std::tan(cg.theta_cone / 2.0f);
+    p.half_rows = ((float)cg.n_rows - 1.0f) / 2.0f;
+    p.taper_scale = (pi / 2.0f) / (1.0f - kQ);
+    p.out_scale = 2.0f * pi / (float)cg.n_proj_turn;
+    if (p.n_rows < 2 || p.nos < 2) {
+        set_error("backproject: detector too small");
+        return CTBB_ERR_ARGUMENT;
+    }
+    dim3 block(32, 8);
+    dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8, 1);
+    switch (zpt) {
+    case 32:
+        grid.z = (p.n_slices + 31) / 32;
+        backproject_kernel<32><<<grid, block, 0, stream>>>(p);
+        break;
+    case 16:
+        grid.z = (p.n_slices + 15) / 16;
+        backproject_kernel<16><<<grid, block, 0, stream>>>(p);
+        break;
+    case 4:
+        grid.z = (p.n_slices + 3) / 4;
+        backproject_kernel<4><<<grid, block, 0, stream>>>(p);
+        break;
+    default:
+        grid.z = (p.n_slices + 7) / 8;
+        backproject_kernel<8><<<grid, block, 0, stream>>>(p);
+        break;
+    }
+    count_launch();
+    CTBB_CUDA_TRY(cudaGetLastError());
+    return CTBB_OK;
+}
+
+}  // namespace ctbb

@@ -1,0 +1,26 @@
+// backproject.h -- host tables and launcher of the FP32 wFBP backprojector.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "ctbb_internal.h"
+
+namespace ctbb {
+
+struct BackprojectTables {
+    float tube_start = 0.0f;
+    int nht = 0;               // half turns in the pull window
+    int n_half = 0;            // n_proj_turn / 2
+    int n_slices = 0;          // slices per block
+    std::vector<float> views;  // [n_half][nht][4] {theta, sin, cos, 0}
+    std::vector<float> zpos;   // [n_slices]
+};
+
+int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables *t);
+int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
+                       const float4 *d_views, const float *d_zpos, const float *d_rebin,
+                       float *d_block, int zpt, cudaStream_t stream);
+
+}  // namespace ctbb

@@ -1,0 +1,264 @@
+// ramp_filter.cu -- reconstruction-kernel convolution of rebinned rows.
+//
+// Computes, for every row x of length N (= n_channels_oversampled), the linear
+// convolution y[l] = sum_{k<N} f[N + l - k] x[k] with the 2N-tap kernel f
+// (centre tap at index N), which is what the reference's filter_cpu
+// (src/rebin_filter_cpu.cu:647-709) evaluates through a zero-padded double FFT of
+// size M = 2 * 2^ceil(log2 N), and what its GPU filter kernel
+// (include/rebin_filter.cuh:369-409) evaluates as a direct sum.
+//
+// GB300 design: FP32 FFT convolution entirely in shared memory.  Two real rows
+// are packed into one complex row (x_a + i x_b); because the kernel is real the
+// real and imaginary parts of the inverse transform are the two filtered rows.
+// Each CTA is persistent, loads the twiddle table once and then loops over row
+// pairs: load (coalesced) -> forward Stockham passes (radix 4, one radix-2 pass
+// when log2 M is odd) -> multiply by the kernel spectrum H/M (fused into the
+// first inverse pass) -> inverse passes -> store.  HBM traffic is one read and
+// one write of the rows; the transform lives in shared memory.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <utility>
+#include <vector>
+
+#include "ctbb_internal.h"
+#include "cuda_util.cuh"
+#include "ramp_filter.h"
+
+namespace ctbb {
+
+namespace {
+
+constexpr int kFftThreads = 256;
+
+// Host double-precision radix-2 DFT (bit reversal + butterflies), used once per
+// kernel to compute its spectrum.  data: n interleaved complex values.
+void ctbb_fft_radix2_double(double *data, int n, int sign)
+{
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            std::swap(data[2 * i], data[2 * j]);
+            std::swap(data[2 * i + 1], data[2 * j + 1]);
+        }
+    }
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1;
+        for (int k = 0; k < half; ++k) {
+            double ang = sign * two_pi * (double)k / (double)len;
+            double wr = std::cos(ang), wi = std::sin(ang);
+            for (int s = 0; s < n; s += len) {
+                int a = s + k, b = a + half;
+                double br = data[2 * b] * wr - data[2 * b + 1] * wi;
+                double bi = data[2 * b] * wi + data[2 * b + 1] * wr;
+                data[2 * b] = data[2 * a] - br;
+                data[2 * b + 1] = data[2 * a + 1] - bi;
+                data[2 * a] += br;
+                data[2 * a + 1] += bi;
+            }
+        }
+    }
+}
+
+struct FftParams {
+    float *lines;        // [n_lines][n]
+    size_t n_lines;
+    int n;               // row length
+    int m;               // transform size (power of two)
+    int log2m;
+    const float2 *spectrum;  // H[k] / M, [m]
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// One Stockham pass of radix R over m points, src -> dst.  sign = -1 forward,
+// +1 inverse.  tw[t] = exp(-2 pi i t / m); the inverse uses the conjugate.
+template <int R>
+__device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                              const float2 *__restrict__ tw, int m, int ns, int sign,
+                                              const float2 *__restrict__ pre_mul)
+{
+    const int nb = m / R;
+    const int tstride = m / (ns * R);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        int k = j % ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            v[r] = src[j + r * nb];
+            if (pre_mul) v[r] = cmul(v[r], __ldg(pre_mul + j + r * nb));
+        }
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            float2 w = tw[(r * k * tstride) & (m - 1)];
+            if (sign > 0) w.y = -w.y;
+            v[r] = cmul(v[r], w);
+        }
+        if (R == 2) {
+            float2 a = v[0], b = v[1];
+            v[0] = make_float2(a.x + b.x, a.y + b.y);
+            v[1] = make_float2(a.x - b.x, a.y - b.y);
+        } else {
+            float2 a = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
+            float2 b = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+            float2 c = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
+            float2 e = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
+            // d = e * (sign * i)
+            float2 d = sign < 0 ? make_float2(e.y, -e.x) : make_float2(-e.y, e.x);
+            v[0] = make_float2(a.x + c.x, a.y + c.y);
+            v[2] = make_float2(a.x - c.x, a.y - c.y);
+            v[1] = make_float2(b.x + d.x, b.y + d.y);
+            v[3] = make_float2(b.x - d.x, b.y - d.y);
+        }
+        int base = (j / ns) * ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[base + r * ns] = v[r];
+    }
+}
+
+// Full transform; returns the buffer holding the result.
+__device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int log2m, int sign,
+                            const float2 *pre_mul)
+{
+    int ns = 1;
+    bool first = true;
+    if (log2m & 1) {
+        stockham_pass<2>(a, b, tw, m, ns, sign, pre_mul);
+        __syncthreads();
+        float2 *t = a; a = b; b = t;
+        ns *= 2;
+        first = false;
+    }
+    while (ns < m) {
+        stockham_pass<4>(a, b, tw, m, ns, sign, first ? pre_mul : nullptr);
+        __syncthreads();
+        float2 *t = a; a = b; b = t;
+        ns *= 4;
+        first = false;
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, const float2 *__restrict__ g_tw)
+{
+    extern __shared__ float2 smem[];
+    float2 *tw = smem;
+    float2 *buf_a = smem + p.m;
+    float2 *buf_b = smem + 2 * p.m;
+    for (int i = threadIdx.x; i < p.m; i += blockDim.x) tw[i] = g_tw[i];
+    size_t n_pairs = (p.n_lines + 1) / 2;
+    for (size_t pair = blockIdx.x; pair < n_pairs; pair += gridDim.x) {
+        size_t la = 2 * pair, lb = la + 1;
+        bool has_b = lb < p.n_lines;
+        const float *ra = p.lines + la * (size_t)p.n;
+        const float *rb = p.lines + lb * (size_t)p.n;
+        __syncthreads();  // previous pair's stores done before buf_a is rewritten
+        for (int i = threadIdx.x; i < p.m; i += blockDim.x) {
+            float xa = 0.f, xb = 0.f;
+            if (i < p.n) {
+                xa = ra[i];
+                if (has_b) xb = rb[i];
+            }
+            buf_a[i] = make_float2(xa, xb);
+        }
+        __syncthreads();
+        float2 *res = fft_smem(buf_a, buf_b, tw, p.m, p.log2m, -1, nullptr);
+        float2 *other = (res == buf_a) ? buf_b : buf_a;
+        res = fft_smem(res, other, tw, p.m, p.log2m, +1, p.spectrum);
+        float *wa = p.lines + la * (size_t)p.n;
+        float *wb = p.lines + lb * (size_t)p.n;
+        for (int i = threadIdx.x; i < p.n; i += blockDim.x) {
+            float2 v = res[i];
+            wa[i] = v.x;
+            if (has_b) wb[i] = v.y;
+        }
+    }
+}
+
+}  // namespace
+
+int ramp_transform_size(int n)
+{
+    int m = 1;
+    while (m < n) m <<= 1;
+    return 2 * m;
+}
+
+int prepare_ramp_filter(const float *h_taps, int n, RampFilterPlan *plan, cudaStream_t stream)
+{
+    int m = ramp_transform_size(n);
+    if (m > kMaxRampTransform) {
+        set_error("ramp filter: row length %d needs a %d-point transform (max %d)", n, m,
+                  kMaxRampTransform);
+        return CTBB_ERR_ARGUMENT;
+    }
+    bool same = plan->n == n && plan->taps.size() == (size_t)(2 * n) &&
+                memcmp(plan->taps.data(), h_taps, sizeof(float) * 2 * (size_t)n) == 0;
+    if (same && plan->d_spectrum) return CTBB_OK;
+    plan->n = n;
+    plan->m = m;
+    plan->taps.assign(h_taps, h_taps + 2 * (size_t)n);
+    // Zero-padded kernel as filter_cpu lays it out: F[i] = f[N + i] (i < N),
+    // F[M - N + 1 + t] = f[t + 1] (t < N - 1); H = DFT(F) / M in double.
+    std::vector<double> F(2 * (size_t)m, 0.0);
+    int centre = (int)std::floor((2.0f * n - 1.0f) / 2.0f) + 1;
+    for (int i = 0; i < n; ++i) F[2 * (size_t)i] = h_taps[centre + i];
+    for (int i = m - n + 1; i < m; ++i) F[2 * (size_t)i] = h_taps[i - (m - n + 1) + 1];
+    ctbb_fft_radix2_double(F.data(), m, -1);
+    std::vector<float2> H(m), tw(m);
+    for (int k = 0; k < m; ++k) H[k] = make_float2((float)(F[2 * (size_t)k] / m), (float)(F[2 * (size_t)k + 1] / m));
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int t = 0; t < m; ++t) {
+        double a = -two_pi * (double)t / (double)m;
+        tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    if (!plan->d_spectrum || plan->capacity < (size_t)m) {
+        if (plan->d_spectrum) cudaFree(plan->d_spectrum);
+        plan->d_spectrum = nullptr;
+        CTBB_CUDA_TRY(cudaMalloc(&plan->d_spectrum, sizeof(float2) * 2 * (size_t)m));
+        plan->capacity = (size_t)m;
+    }
+    plan->d_twiddle = plan->d_spectrum + m;
+    CTBB_CUDA_TRY(cudaMemcpyAsync(plan->d_spectrum, H.data(), sizeof(float2) * m, cudaMemcpyHostToDevice, stream));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(plan->d_twiddle, tw.data(), sizeof(float2) * m, cudaMemcpyHostToDevice, stream));
+    // the host vectors die at return: make the copies complete first
+    CTBB_CUDA_TRY(cudaStreamSynchronize(stream));
+    return CTBB_OK;
+}
+
+int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_lines, cudaStream_t stream)
+{
+    if (n_lines == 0) return CTBB_OK;
+    FftParams p;
+    p.lines = d_lines;
+    p.n_lines = n_lines;
+    p.n = plan.n;
+    p.m = plan.m;
+    p.log2m = 0;
+    while ((1 << p.log2m) < p.m) p.log2m++;
+    p.spectrum = plan.d_spectrum;
+    size_t smem = sizeof(float2) * 3 * (size_t)p.m;
+    static bool attr_set = false;
+    if (!attr_set) {
+        CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(float2) * 3 * kMaxRampTransform)));
+        attr_set = true;
+    }
+    int per_sm = (int)std::max<size_t>(1, (size_t)(200 * 1024) / smem);
+    if (per_sm > 4) per_sm = 4;
+    size_t n_pairs = (n_lines + 1) / 2;
+    int grid = (int)std::min<size_t>(n_pairs, (size_t)num_sms() * per_sm);
+    ramp_fft_kernel<<<grid, kFftThreads, smem, stream>>>(p, plan.d_twiddle);
+    count_launch();
+    CTBB_CUDA_TRY(cudaGetLastError());
+    return CTBB_OK;
+}
+
+}  // namespace ctbb

@@ -1,0 +1,46 @@
+// rebin.h -- host tables and launcher of the FFS / fan-to-parallel rebinning.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "ctbb_internal.h"
+
+namespace ctbb {
+
+enum class RebinMode { kNoFfs, kPhiFfs, kZFfs, kBothFfs };
+
+// interp3 taps along one axis (base, aliased upper tap, weight, 1 - weight).
+struct AxisTap {
+    int i0, i1;
+    float u, one_minus_u;
+};
+
+// View-axis term of one (focal spot, channel): beta * n_proj_ffs / (2 pi).
+struct FocalTerm {
+    float t_alpha;
+};
+
+struct RebinTables {
+    RebinMode mode = RebinMode::kNoFfs;
+    int n_ffs = 1, n_channels = 0, n_os = 0, n_rows_raw = 0, n_rows = 0;
+    int n_proj = 0, add_projections = 0, n_views = 0, reverse_rows = 0;
+    std::vector<AxisTap> out_taps;   // [side][n_os]
+    std::vector<FocalTerm> focal;    // no/z-FFS: [side][n_os]; phi/both: [focal][n_channels]
+    std::vector<float> focal_offset; // d_alpha_r * n_proj_ffs / (2 pi) per focal spot
+};
+
+struct DeviceRebinTables {
+    void *base = nullptr;
+    size_t capacity = 0;
+    AxisTap *taps = nullptr;
+    FocalTerm *focal = nullptr;
+};
+
+int build_rebin_tables(const struct recon_metadata &mr, RebinTables *t);
+int upload_rebin_tables(const RebinTables &t, DeviceRebinTables *dt, cudaStream_t stream);
+int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float *d_raw,
+                 float *d_out, cudaStream_t stream);
+
+}  // namespace ctbb

@@ -1,0 +1,365 @@
+/*
+ * ctbb_gb300.h -- C ABI of the GB300 helical weighted-FBP library.
+ *
+ * Two layers are declared here.
+ *
+ *  1. The boundary types.  struct recon_params, struct recon_info, struct ct_data,
+ *     struct ct_geom, struct flags and struct recon_metadata have the same field
+ *     names, types and order as the CTBangBang types they stand in for
+ *     (include/parse_config.h:36-67 and include/recon_structs.h:26-113 of the
+ *     reference), so a driver written against the reference's headers passes the
+ *     same bytes to this library.
+ *
+ *  2. Entry points.  Every extern "C" function returns a ctbb_status (0 = success)
+ *     and never calls exit().  Under C++ the header also declares the four
+ *     reference module functions with their original C++ linkage
+ *     (adaptive_filter_kk, rebin_filter, backproject, finalize_image_stack), so a
+ *     driver that follows the reference main.cu call order links unchanged.
+ *
+ * Data layouts (all float32, C order, fastest index last):
+ *   raw     [n_proj_pull][n_rows_raw][n_channels]              host, ctd.raw
+ *   rebin   [n_views][n_rows][n_channels_oversampled]           device, ctd.d_rebin
+ *           n_views = n_proj_pull/n_ffs - 2*add_projections
+ *   image   [n_slices_recon][ny][nx]                            host, ctd.image
+ *   final   [n_slices_final][ny][nx]                            host, ctd.final_image_stack
+ *
+ * Threading: calls on one recon_metadata are not reentrant (the reference's are
+ * not either).  Device work runs on the stream set by ctbb_set_stream (default:
+ * the legacy default stream) and every drop-in call returns after that stream is
+ * synchronised, as the reference's blocking cudaMemcpy calls did.
+ */
+#ifndef CTBB_GB300_H
+#define CTBB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+/* ------------------------------------------------------------------------- */
+/* Boundary types (layout of the reference's parse_config.h / recon_structs.h) */
+/* ------------------------------------------------------------------------- */
+
+#ifndef CTBB_REFERENCE_STRUCTS_DEFINED
+#define CTBB_REFERENCE_STRUCTS_DEFINED
+
+/* .prm keys, parse_config.h:36-67 of the reference. */
+struct recon_params {
+    char raw_data_dir[4096];
+    char raw_data_file[255];
+    char output_dir[4096];
+    char output_file[255];
+    int n_rows;                 /* Nrows: detector rows after z-FFS            */
+    float coll_slicewidth;      /* CollSlicewidth [mm at isocentre]            */
+    float start_pos;            /* StartPos [mm]                               */
+    float end_pos;              /* EndPos [mm]                                 */
+    float pitch_value;          /* PitchValue / TableFeed: feed per turn [mm]  */
+    float slice_thickness;      /* SliceThickness [mm]                         */
+    float acq_fov;              /* AcqFOV [mm]                                 */
+    float recon_fov;            /* ReconFOV [mm]                               */
+    int recon_kernel;           /* ReconKernel: -100 ramp, -1,1,2,3, else b<k> */
+    int n_readings;             /* Readings: frames in the raw file            */
+    float x_origin;             /* Xorigin [mm]                                */
+    float y_origin;             /* Yorigin [mm]                                */
+    int z_ffs;                  /* Zffs                                        */
+    int phi_ffs;                /* Phiffs                                      */
+    char scanner[4351];         /* Scanner: .scanner path or 0/1/2             */
+    int file_type;              /* FileType (0 = float32 binary frames)        */
+    int file_subtype;           /* FileSubType                                 */
+    int raw_data_offset;        /* RawOffset [bytes]                           */
+    unsigned int nx;            /* Nx                                          */
+    unsigned int ny;            /* Ny                                          */
+    float tube_start_angle;     /* TubeStartAngle [deg]                        */
+    float adaptive_filtration_s;/* AdaptiveFiltration strength                 */
+    int n_slices;               /* NSlices (overrides EndPos when non-zero)    */
+    char table_dir_str[1024];   /* TableDir: "in" / "out"                      */
+    int table_dir;              /* TableDirInt: -1 in, 1 out                   */
+};
+
+struct block_info {
+    int block_idx;
+    float block_slice_start;
+    float block_slice_end;
+    int idx_block_slice_start;
+    int idx_block_slice_end;
+};
+
+struct recon_info {
+    size_t n_ffs;
+    float data_begin_pos;
+    float data_end_pos;
+    float allowed_begin;
+    float allowed_end;
+    size_t n_slices_requested;
+    size_t n_slices_recon;
+    size_t n_slices_block;
+    size_t n_blocks;
+    size_t idx_slice_start;
+    size_t idx_slice_end;
+    float recon_start_pos;
+    float recon_end_pos;
+    size_t idx_pull_start;
+    size_t idx_pull_end;
+    size_t n_proj_pull;
+    struct block_info cb;
+};
+
+struct ct_data {
+    float *raw;
+    float *rebin;
+    float *image;
+    float *d_raw;
+    float *d_rebin;
+    float *d_image;
+    float *d_final_image_stack;
+    float *final_image_stack;
+};
+
+struct ct_geom {
+    size_t n_proj_turn;
+    size_t n_proj_ffs;
+    size_t n_channels;
+    size_t n_channels_oversampled;
+    size_t n_rows;
+    size_t n_rows_raw;
+    float r_f;
+    float z_rot;
+    float theta_cone;
+    float fan_angle_increment;
+    float src_to_det;
+    float anode_angle;
+    float central_channel;
+    float acq_fov;
+    size_t projection_offset;
+    size_t add_projections;
+    size_t add_projections_ffs;
+    int reverse_row_interleave;
+    int reverse_channel_interleave;
+    int table_direction;        /* -1 table positions decreasing, 1 increasing */
+};
+
+struct flags {
+    int testing;
+    int verbose;
+    int no_gpu;
+    int set_device;
+    int device_number;
+    int timing;
+    int benchmark;
+};
+
+struct recon_metadata {
+    char home_dir[4096];
+    char cwd[4096];
+    char install_dir[4096];
+    struct flags flags;
+    struct recon_params rp;
+    struct recon_info ri;
+    struct ct_geom cg;
+    struct ct_data ctd;
+    float *tube_angles;
+    double *table_positions;
+};
+
+#endif /* CTBB_REFERENCE_STRUCTS_DEFINED */
+
+/* ------------------------------------------------------------------------- */
+/* Status codes                                                              */
+/* ------------------------------------------------------------------------- */
+
+typedef enum ctbb_status {
+    CTBB_OK = 0,
+    CTBB_ERR_ARGUMENT = 1,      /* null pointer, zero size, unsupported value    */
+    CTBB_ERR_CONFIG = 2,        /* .prm / .scanner key missing or inconsistent   */
+    CTBB_ERR_RANGE = 3,         /* recon range outside the allowed data range    */
+    CTBB_ERR_IO = 4,            /* file not found / short read / write failed    */
+    CTBB_ERR_CUDA = 5,          /* a CUDA runtime call failed (see last error)   */
+    CTBB_ERR_NO_DEVICE = 6,     /* no CUDA device: the library has no CPU path   */
+    CTBB_ERR_ALLOC = 7,         /* host or device allocation failed              */
+    CTBB_ERR_STATE = 8          /* call out of order (e.g. backproject w/o rebin) */
+} ctbb_status;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Human-readable text of the last error on this thread ("" if none). */
+const char *ctbb_last_error(void);
+
+/* Library version string. */
+const char *ctbb_version(void);
+
+/* Stream on which all device work of the following calls is issued
+   (a cudaStream_t passed as void*; NULL = legacy default stream). */
+int ctbb_set_stream(void *stream);
+
+/* ------------------------------------------------------------------------- */
+/* Planner (host).  Bit-exact restatements of the reference's integer tables. */
+/* ------------------------------------------------------------------------- */
+
+/* Parse a .prm file into *rp and apply the TableDir defaults and the
+   required-key checks.  Replaces configure_recon_params, src/setup.cu:108-176
+   (and parse_config, src/parse_config.cu:40-217).  Returns CTBB_ERR_CONFIG
+   instead of exit(1) when a required key is missing. */
+int ctbb_configure_recon_params(const char *prm_path, struct recon_params *rp);
+
+/* Fill mr->cg from mr->rp.scanner (a .scanner file path, a file name under
+   <install_dir>/resources/scanners, or the built-in scanners "0", "1", "2").
+   Replaces configure_ct_geom, src/setup.cu:178-383. */
+int ctbb_configure_ct_geom(struct recon_metadata *mr);
+
+/* Per-frame tube angle / table position tables for FileType 0, the recon slice
+   range, block count and first pull window; allocates mr->tube_angles,
+   mr->table_positions, mr->ctd.raw, mr->ctd.rebin and mr->ctd.image (calloc).
+   Replaces configure_reconstruction, src/setup.cu:385-603.  The raw file is
+   not opened; CTBB_ERR_RANGE replaces the reference's exit(1). */
+int ctbb_configure_reconstruction(struct recon_metadata *mr);
+
+/* Next 32-slice block: pull window, block slice range, block_idx++ and
+   re-allocation of ctd.raw / ctd.rebin.  Replaces update_block_info,
+   src/setup.cu:605-679. */
+int ctbb_update_block_info(struct recon_metadata *mr);
+
+/* Read the block's pull window of FileType-0 frames (float32, little endian,
+   RawOffset bytes of header) into ctd.raw; frames past the end of the file read
+   as zeros.  Replaces extract_projections, src/setup.cu:681-767 (type 0 only). */
+int ctbb_extract_projections(struct recon_metadata *mr);
+
+/* Write the float32 final stack to <output_dir>/<output_file> and free every
+   host array the planner and finalize allocated.  Replaces finish_and_cleanup,
+   src/setup.cu:769-787. */
+int ctbb_finish_and_cleanup(struct recon_metadata *mr);
+
+/* Number of final slices: floor(|end-start|/slice_thickness)+1
+   (src/finalize_image_stack_cpu.cu:67). */
+int ctbb_n_slices_final(const struct recon_metadata *mr);
+
+/* Load the 2*n_channels_oversampled float32 reconstruction-kernel taps named by
+   rp.recon_kernel from <install_dir>/resources/filters/f_<N>_<name>.txt.  For
+   ReconKernel -100 a missing f_<N>_ramp.txt is generated from the ramp formula
+   (ctbb_ramp_filter_taps).  Replaces load_filter, src/rebin_filter.cu:922-959. */
+int ctbb_load_filter(const struct recon_metadata *mr, float *taps_out);
+
+/* Ramp/apodised kernel taps f[j], j in [0, 2*n_os): f = (c^2/(2 ds)) *
+   (a r(c pi k) + (1-a)/2 r(c pi k + pi) + (1-a)/2 r(c pi k - pi)), k = j - n_os,
+   r(t) = sin t/t + (cos t - 1)/t^2, r(0) = 1/2, ds = r_f sin(fan_angle_inc/2)
+   (resources/ramp.m of the reference). */
+int ctbb_ramp_filter_taps(int n_os, float ds, float c, float a, float *taps_out);
+
+/* ------------------------------------------------------------------------- */
+/* Hot path: drop-in module functions (host buffers, reference semantics).    */
+/* ------------------------------------------------------------------------- */
+
+/* Kachelriess-Kalender adaptive raw-data filter on ctd.raw, in place.
+   Replaces adaptive_filter_kk, src/preprocessing.cu:31-156 / include/preprocessing.h:26. */
+int ctbb_adaptive_filter_kk(struct recon_metadata *mr);
+
+/* FFS + fan-to-parallel rebinning and ramp filtering of ctd.raw.  The result is
+   left on the device in ctd.d_rebin (cudaMalloc'd here, freed by
+   ctbb_backproject), as the reference does.  If mr->flags.testing is set the
+   result is also copied to the host array ctd.rebin.
+   Replaces rebin_filter, src/rebin_filter.cu:38-56 / include/rebin_filter.h:27. */
+int ctbb_rebin_filter(struct recon_metadata *mr);
+
+/* Weighted-FBP backprojection of ctd.d_rebin into the 32-slice block
+   ctd.image[(cb.block_idx-1)*nx*ny*32 ...], CPU-path conventions
+   (src/backproject_cpu.cu:49-154).  Frees ctd.d_rebin.
+   Replaces backproject, src/backproject.cu:31-108 / include/backproject.h:26. */
+int ctbb_backproject(struct recon_metadata *mr);
+
+/* Block reorder + triangle slice thickening of ctd.image into a newly
+   calloc'd ctd.final_image_stack (attenuation units, as the reference).
+   Replaces finalize_image_stack, src/finalize_image_stack.cu:26-120 /
+   include/finalize_image_stack.h:26 (CPU twin src/finalize_image_stack_cpu.cu:24-117). */
+int ctbb_finalize_image_stack(struct recon_metadata *mr);
+
+/* As ctbb_finalize_image_stack, then HU = 1000 (mu - mu_water) / mu_water.
+   No counterpart in the reference (it has no HU conversion). */
+int ctbb_finalize_image_stack_hu(struct recon_metadata *mr, float mu_water);
+
+/* ------------------------------------------------------------------------- */
+/* Hot path: device-resident stages (device pointers, asynchronous on the     */
+/* library stream).  These are what the drop-in functions call.              */
+/* ------------------------------------------------------------------------- */
+
+/* Adaptive filter of one pull window: d_raw_in -> d_raw_out (distinct buffers,
+   [n_proj_pull][n_rows_raw][n_channels]).  Uses mr->cg, mr->ri, mr->rp. */
+int ctbb_adaptive_filter_device(const struct recon_metadata *mr,
+                                const float *d_raw_in, float *d_raw_out);
+
+/* Rebin (no filter) of one pull window into d_rebin [n_views][n_rows][n_os]. */
+int ctbb_rebin_device(const struct recon_metadata *mr, const float *d_raw,
+                      float *d_rebin);
+
+/* Ramp filter of n_lines rows of length n_os in place, taps of length 2*n_os. */
+int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os,
+                            const float *h_taps);
+
+/* Backprojection of one block of filtered rebinned views into
+   d_block [n_slices_block][ny][nx] (overwritten). */
+int ctbb_backproject_device(const struct recon_metadata *mr,
+                            const float *d_rebin, float *d_block);
+
+/* Reorder + thicken d_image [n_slices_recon][ny][nx] into
+   d_final [n_slices_final][ny][nx]; mu_water > 0 also converts to HU. */
+int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image,
+                         float *d_final, float mu_water);
+
+/* Whole scan, device resident: every 32-slice block of the plan in *mr
+   (re-planned with the reference's update_block_info per block) from the full
+   raw scan d_scan [n_readings][n_rows_raw][n_channels] into
+   d_final [n_slices_final][ny][nx].  mr->ri.cb.block_idx is reset to 0 first and
+   advanced as in the reference block loop.  Work buffers are cached inside the
+   library between calls. */
+int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
+                            float *d_final, float mu_water);
+
+/* Bytes of device workspace ctbb_reconstruct_device keeps for this plan. */
+size_t ctbb_workspace_bytes(const struct recon_metadata *mr);
+
+/* Release every cached device buffer of the library. */
+int ctbb_release_workspace(void);
+
+/* Number of kernels this library launched since load (all entry points). */
+uint64_t ctbb_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------- */
+/* Synthetic helical phantom (test and benchmark input; not on the hot path). */
+/* ------------------------------------------------------------------------- */
+
+/* One phantom object: an ellipsoid (kind 1) or an infinite z-cylinder (kind 0)
+   with attenuation mu (added to what lies beneath) [1/mm]. */
+struct ctbb_phantom_object {
+    int kind;
+    float mu;
+    float center[3];
+    float semi_axes[3];
+    float rotation[9];          /* row-major world->body rotation */
+};
+
+/* Forward-project n_objects into frames [frame0, frame0+n_frames) of a helical
+   FFS scan described by mr->cg / mr->rp and the tables mr->tube_angles,
+   mr->table_positions (length rp.n_readings).  i0 > 0 adds Poisson noise with
+   that unattenuated count (seeded; counter-based so host and device agree
+   up to libm rounding).  out: [n_frames][n_rows_raw][n_channels] line integrals.
+   The host variant runs on the CPU; the device variant takes device pointers
+   for out and the two tables. */
+int ctbb_phantom_project_host(const struct recon_metadata *mr,
+                              const struct ctbb_phantom_object *objects, int n_objects,
+                              size_t frame0, size_t n_frames, float i0, uint64_t seed,
+                              float *out);
+int ctbb_phantom_project_device(const struct recon_metadata *mr,
+                                const struct ctbb_phantom_object *objects, int n_objects,
+                                const float *d_tube_angles, const double *d_table_positions,
+                                size_t frame0, size_t n_frames, float i0, uint64_t seed,
+                                float *d_out);
+
+#ifdef __cplusplus
+} /* extern "C" */
+
+/* C++-linkage drop-ins with the reference's exact signatures. */
+int adaptive_filter_kk(struct recon_metadata *mr);   /* include/preprocessing.h:26 */
+int rebin_filter(struct recon_metadata *mr);         /* include/rebin_filter.h:27 */
+int backproject(struct recon_metadata *mr);          /* include/backproject.h:26 */
+int finalize_image_stack(struct recon_metadata *mr); /* include/finalize_image_stack.h:26 */
+#endif
+
+#endif /* CTBB_GB300_H */
