@@ -1,0 +1,539 @@
+"""Benchmark of the helical weighted-FBP hot path on one (or N replica) GB300s.
+
+A step is one full reconstruction of the config-2 scan (736 channels x 32
+raw rows, phi+z flying focal spot rebinned to 1472 x 64, 1152 views/turn,
+pitch 0.8, 10 turns, 512^2 x 96 raw slices in 3 blocks of 32, thickened to
+16 final 3 mm slices): per block adaptive raw filter -> FFS rebin -> ramp
+filter -> FP32 wFBP backprojection, then reorder/thicken.  Input: a seeded
+synthetic phantom scan (water cylinder + 30 ellipsoids, Poisson noise at
+I0 = 5e4) generated on the device; there is no public dataset.
+
+  value  voxel-updates/s with the raw scan resident in HBM (device-timed with
+         CUDA events on the library's stream); 4.3 GB of raw input per step is
+         larger than L2, so no flush is needed between steps.
+  e2e    the same metric through ctbb_reconstruct_host from pinned host
+         buffers: each block's pull window is copied host->device and the final
+         stack device->host inside the timed region.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import concurrent.futures as cf
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+FLOP_PER_VU = 13          # q FMA 2, q_idx FMA 2, bilinear 6, s += W v 2, h += W 1
+STAGES = ["adaptive_filter", "rebin", "ramp_filter", "backproject", "finalize"]
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="config2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one block of the config through each stage once (small case for ncu captures)")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+# plan and sizes
+# --------------------------------------------------------------------------
+
+def make_plan(spec, workdir):
+    from ctbangbang_gb300 import scans
+    prm, inst = scans.prepare(spec, workdir)
+    return scans.plan(prm, inst)
+
+
+def block_plans(mr):
+    """recon_info of every block (the reference's update_block_info sequence)."""
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import structs
+    m = structs.ReconMetadata()
+    C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+    m.ctd.raw = m.ctd.rebin = None
+    m.ri.cb.block_idx = 0
+    out = []
+    for _ in range(mr.ri.n_blocks):
+        L.call("ctbb_update_block_info", C.byref(m))
+        ri = structs.ReconInfo()
+        C.memmove(C.byref(ri), C.byref(m.ri), C.sizeof(ri))
+        out.append(ri)
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    libc.free(C.cast(m.ctd.raw, C.c_void_p))
+    libc.free(C.cast(m.ctd.rebin, C.c_void_p))
+    return out
+
+
+def workload_sizes(mr, blocks):
+    nht = [(ri.n_proj_pull // ri.n_ffs - 2 * mr.cg.add_projections) // (mr.cg.n_proj_turn // 2) for ri in blocks]
+    plane = mr.rp.nx * mr.rp.ny
+    vu_blocks = [plane * mr.ri.n_slices_block * (mr.cg.n_proj_turn // 2) * k for k in nht]
+    frame = mr.cg.n_rows_raw * mr.cg.n_channels
+    n_readings = mr.rp.n_readings
+    h2d = 0
+    for ri in blocks:
+        s = int(ri.idx_pull_start)
+        s = s - 2 ** 64 if s >= 2 ** 63 else s
+        a, e = max(s, 0), min(s + ri.n_proj_pull, n_readings)
+        h2d += max(e - a, 0) * frame * 4
+    return dict(nht=nht, vu_per_block=vu_blocks, vu_total=sum(vu_blocks), h2d_bytes=h2d,
+                raw_samples=[ri.n_proj_pull * frame for ri in blocks],
+                rebin_samples=[(ri.n_proj_pull // ri.n_ffs - 2 * mr.cg.add_projections) * mr.cg.n_rows *
+                               mr.cg.n_channels_oversampled for ri in blocks])
+
+
+# --------------------------------------------------------------------------
+# clocks
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="ctbb_clocks_", suffix=".csv")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.remove(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle port (the reference CPU path's algorithm) on host cores
+# --------------------------------------------------------------------------
+
+def cpu_baseline(spec, mr, blocks, sizes, threads=None, steps=1, warmup=0, sub_frames=1024, angles_per_thread=1):
+    """Bounded sample of the whole step on every host core: each thread runs
+    (a) adaptive filter + FFS rebin + ramp filter of its own 1024-frame
+    sub-window of block 0 and (b) the backprojection of one half-turn angle of
+    block 0 (512^2 x 32 voxels x n_half_turns).  The full-scan CPU time is
+    composed from the per-frame and per-angle rates of those samples; VU/s is
+    that scan's voxel updates over the composed time."""
+    from ctbangbang_gb300 import scans, structs
+    from oracle import oracle as O
+    orc = O.oracle()
+    T = threads or os.cpu_count() or 1
+    frame = mr.cg.n_rows_raw * mr.cg.n_channels
+    b0 = blocks[0]
+    # host raw of T distinct sub-windows (generated on the CPU)
+    subs = []
+    objs = scans.phantom_objects(spec)
+    s0 = int(b0.idx_pull_start)
+
+    def gen(t):
+        start = s0 + (t * sub_frames) % max(b0.n_proj_pull - sub_frames, 1)
+        start -= start % mr.ri.n_ffs
+        return scans.project_host(mr, objs, start, sub_frames, spec.i0, spec.seed)
+
+    with cf.ThreadPoolExecutor(T) as ex:
+        subs = list(ex.map(gen, range(T)))
+
+    def sub_meta(raw):
+        m = structs.ReconMetadata()
+        C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+        m.ri = b0
+        m.ri.n_proj_pull = sub_frames
+        nv = sub_frames // m.ri.n_ffs - 2 * m.cg.add_projections
+        rb = np.zeros(nv * m.cg.n_rows * m.cg.n_channels_oversampled, np.float32)
+        r = raw.reshape(-1).copy()
+        m.ctd.raw = r.ctypes.data_as(C.POINTER(C.c_float))
+        m.ctd.rebin = rb.ctypes.data_as(C.POINTER(C.c_float))
+        return m, r, rb
+
+    # block-0 filtered rows for the backprojection sample (values do not
+    # change the CPU cost; real pages are touched)
+    mb = structs.ReconMetadata()
+    C.memmove(C.byref(mb), C.byref(mr), C.sizeof(mb))
+    mb.ri = b0
+    rebin_full = np.full(sizes["rebin_samples"][0], 0.01, np.float32)
+    n_half = mr.cg.n_proj_turn // 2
+
+    def run_a(t):
+        m, r, rb = sub_meta(subs[t])
+        orc.oracle_adaptive_filter(C.byref(m))
+        orc.oracle_rebin_filter(C.byref(m))
+        return 0
+
+    def run_b(t):
+        out = np.zeros(mr.rp.nx * mr.rp.ny * mr.ri.n_slices_block, np.float32)
+        i0 = (t * 37) % n_half
+        orc.oracle_backproject_range(C.byref(mb), rebin_full.ctypes.data_as(C.POINTER(C.c_float)), i0,
+                                     i0 + angles_per_thread, out.ctypes.data_as(C.POINTER(C.c_float)))
+        return 0
+
+    results = []
+    for it in range(warmup + steps):
+        with cf.ThreadPoolExecutor(T) as ex:
+            t0 = time.perf_counter()
+            list(ex.map(run_a, range(T)))
+            ta = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            list(ex.map(run_b, range(T)))
+            tb = time.perf_counter() - t0
+        if it >= warmup:
+            per_frame = ta / (T * sub_frames)                  # s per raw frame (a), all cores busy
+            per_angle = tb / (T * angles_per_thread)          # s per half-turn angle (b)
+            scan_s = sum(ri.n_proj_pull for ri in blocks) * per_frame + len(blocks) * n_half * per_angle
+            results.append(dict(value=sizes["vu_total"] / scan_s, scan_s=scan_s, ta=ta, tb=tb))
+    best = statistics.median(r["value"] for r in results)
+    sample = ("%d threads; per step each thread: adaptive filter + phi/z-FFS rebin + ramp filter of a "
+              "%d-frame sub-window of block 0, then the backprojection of %d half-turn angle(s) of block 0 "
+              "(512^2 x 32 voxels x %d half turns); full-scan time composed from those per-frame and "
+              "per-angle rates over the %d frames and %d angles of the 3-block scan (finalize omitted, "
+              "< 0.1%% of the CPU time)" % (T, sub_frames, angles_per_thread, sizes["nht"][0],
+                                           sum(ri.n_proj_pull for ri in blocks), len(blocks) * n_half))
+    return dict(value=best, unit="voxel-updates/s", cores=T, kind="port", sample=sample,
+                scan_seconds=statistics.median(r["scan_s"] for r in results))
+
+
+# --------------------------------------------------------------------------
+# reference arm
+# --------------------------------------------------------------------------
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from ctbangbang_gb300 import scans
+    spec = scans.CONFIGS[args.config]
+    with tempfile.TemporaryDirectory(prefix="ctbb_bench_") as d:
+        mr = make_plan(spec, d)
+        blocks = block_plans(mr)
+        sizes = workload_sizes(mr, blocks)
+        warm = max(args.warmup, 3) if args.warmup else 0
+        t0 = time.perf_counter()
+        cb = cpu_baseline(spec, mr, blocks, sizes, steps=args.steps, warmup=min(warm, 1))
+        wall = time.perf_counter() - t0
+        scans.free_plan(mr)
+    v = cb["value"]
+    line = {
+        "impl": "reference", "metric": "voxel-updates/s", "value": v, "unit": "voxel-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cb["scan_seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded helical phantom (config-2 geometry)",
+        "config": {"workload": "%s: full-FFS helical wFBP, 3 blocks of 512^2 x 32" % args.config,
+                   "voxel_updates_per_scan": sizes["vu_total"], "scans_per_s": 1.0 / cb["scan_seconds"],
+                   "wall_s": wall,
+                   "note": "reference CPU path as restated bit-exactly by the oracle port (the reference's "
+                           "own sources build only where the reference tree is present)"},
+        "cpu_baseline": {"value": v, "unit": "voxel-updates/s", "cores": cb["cores"], "kind": "port",
+                         "sample": cb["sample"]},
+        "e2e": {"value": v, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+
+def read_traffic():
+    p = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return {}
+    return {}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)), "measured"
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_ours(args):
+    import torch
+
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = L.load()
+    lib.ctbb_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    spec = scans.CONFIGS[args.config]
+    tmp = tempfile.TemporaryDirectory(prefix="ctbb_bench_")
+    mr = make_plan(spec, tmp.name)
+    blocks = block_plans(mr)
+    sizes = workload_sizes(mr, blocks)
+    n = spec.n_readings
+    frame = mr.cg.n_rows_raw * mr.cg.n_channels
+    plane = mr.rp.nx * mr.rp.ny
+    n_final = lib.ctbb_n_slices_final(C.byref(mr))
+
+    # synthetic scan on the device (each replica its own seed)
+    ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
+    tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
+    objs = scans.phantom_objects(spec)
+    d_scan = torch.empty(n * frame, dtype=torch.float32, device="cuda")
+    L.call("ctbb_phantom_project_device", C.byref(mr), objs, len(objs), C.c_void_p(ta.data_ptr()),
+           C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), spec.seed + 7919 * rank,
+           C.c_void_p(d_scan.data_ptr()))
+    d_final = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
+
+    def step():
+        L.call("ctbb_reconstruct_device", C.byref(mr), C.c_void_p(d_scan.data_ptr()),
+               C.c_void_p(d_final.data_ptr()), C.c_float(0.0))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local) if rank == 0 else None
+    lib.ctbb_profile_read(None, None, 0, 1)
+    lib.ctbb_profile_enable(1)
+    launches0 = lib.ctbb_kernel_launch_count()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record()
+    for k in range(args.steps):
+        step()
+        ev[k + 1].record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    launches = lib.ctbb_kernel_launch_count() - launches0
+    lib.ctbb_profile_enable(0)
+    stage_ms = (C.c_double * 5)()
+    stage_n = (C.c_uint64 * 5)()
+    lib.ctbb_profile_read(stage_ms, stage_n, 5, 1)
+    clk = clocks.stop() if clocks else None
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    ms = total_ms / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * sizes["vu_total"] / (ms * 1e-3)
+
+    # e2e through the host-buffer entry point (pinned host scan and stack)
+    e2e = None
+    if not args.no_e2e:
+        h_scan = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
+        h_scan.copy_(d_scan)
+        h_final = torch.empty(n_final * plane, dtype=torch.float32, pin_memory=True)
+        hp = h_scan.numpy().ctypes.data_as(C.POINTER(C.c_float))
+        fp = h_final.numpy().ctypes.data_as(C.POINTER(C.c_float))
+
+        def e2e_step():
+            L.call("ctbb_reconstruct_host", C.byref(mr), hp, fp, C.c_float(0.0))
+
+        for _ in range(2):
+            e2e_step()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        if dist is not None:
+            t = torch.tensor([e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        same = bool(torch.equal(h_final.cuda(), d_final))
+        e2e = {"value": world * sizes["vu_total"] / (e_ms * 1e-3), "unit": "voxel-updates/s",
+               "h2d_bytes_per_step": sizes["h2d_bytes"], "d2h_bytes_per_step": n_final * plane * 4,
+               "ms_per_step": e_ms, "matches_device_path": same}
+        del h_scan, h_final
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel (backprojection, FP32-pipe bound)
+    peak_fp32 = lib.ctbb_fp32_peak_tflops(5)
+    bp_ms, bp_n = stage_ms[3], max(stage_n[3], 1)
+    vu_per_launch = sizes["vu_total"] / len(blocks)
+    bp_launch_ms = bp_ms / bp_n
+    achieved = FLOP_PER_VU * vu_per_launch / (bp_launch_ms * 1e-3) / 1e12
+    traffic = read_traffic().get("backproject")
+    peaks, peak_kind = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # HBM-bound stages: algorithmic bytes per launch over their measured time
+    nblk = len(blocks)
+    raw_b = sum(sizes["raw_samples"]) / nblk
+    rb_b = sum(sizes["rebin_samples"]) / nblk
+    stage_bytes = {"adaptive_filter": 8 * raw_b, "rebin": 4 * raw_b + 4 * rb_b, "ramp_filter": 8 * rb_b,
+                   "finalize": 4 * plane * (mr.ri.n_slices_recon + n_final)}
+    stages = {}
+    for i, name in enumerate(STAGES):
+        if stage_n[i] == 0:
+            continue
+        t_launch = stage_ms[i] / stage_n[i]
+        entry = {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_n[i] / args.steps,
+                 "share": stage_ms[i] / max(sum(stage_ms), 1e-9)}
+        if name in stage_bytes:
+            gbs = stage_bytes[name] / (t_launch * 1e-3) / 1e9
+            entry.update({"achieved_gbs": gbs, "frac_of_hbm": gbs / hbm})
+        stages[name] = entry
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(spec, mr, blocks, sizes, steps=1, warmup=0)
+    per_step_sorted = sorted(per_step)
+    line = {
+        "metric": "voxel-updates/s", "value": value, "unit": "voxel-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic seeded helical phantom (config-2 geometry), generated on the device",
+        "config": {
+            "workload": "%s: 736 ch x 32 rows phi+z FFS -> 1472 x 64, 1152 views/turn, pitch 0.8, 10 turns, "
+                        "512^2 x 96 slices (3 blocks) thickened to %d x 3 mm; adaptive filter on" % (args.config, n_final),
+            "scans_per_s": world / (ms * 1e-3),
+            "voxel_updates_per_scan": sizes["vu_total"],
+            "latency_ms": {"p50": per_step_sorted[len(per_step) // 2],
+                           "p99": per_step_sorted[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]},
+            "l2": "no flush: each step reads a 4.3 GB raw scan (> 129 MB L2)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "roofline": {"kernel": "backproject_kernel", "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
+                     "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 > 0 else None,
+                     "traffic": traffic, "flop_per_vu": FLOP_PER_VU, "vu_per_launch": vu_per_launch,
+                     "launch_ms": bp_launch_ms,
+                     "peak_source": "measured FFMA-loop throughput of this GPU in this run "
+                                    "(MEASURED_PEAKS.json has no FP32 figure)"},
+        "stages": stages,
+        "hbm_peak_gbs": hbm, "hbm_peak_kind": peak_kind,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches / args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    scans.free_plan(mr)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_profile_case(args):
+    """Block 0 of the config: its pull window generated on the device, then
+    adaptive filter, rebin, ramp filter and backprojection once each (about
+    2 GB on the device; every input is larger than L2)."""
+    import torch
+
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans, structs
+    lib = L.load()
+    spec = scans.CONFIGS[args.config]
+    tmp = tempfile.TemporaryDirectory(prefix="ctbb_prof_")
+    mr = make_plan(spec, tmp.name)
+    b0 = block_plans(mr)[0]
+    m = structs.ReconMetadata()
+    C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+    m.ri = b0
+    n = spec.n_readings
+    frame = m.cg.n_rows_raw * m.cg.n_channels
+    P = b0.n_proj_pull
+    nv = P // b0.n_ffs - 2 * m.cg.add_projections
+    ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
+    tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
+    objs = scans.phantom_objects(spec)
+    d_raw = torch.empty(P * frame, dtype=torch.float32, device="cuda")
+    L.call("ctbb_phantom_project_device", C.byref(m), objs, len(objs), C.c_void_p(ta.data_ptr()),
+           C.c_void_p(tp.data_ptr()), int(b0.idx_pull_start), P, C.c_float(spec.i0), spec.seed,
+           C.c_void_p(d_raw.data_ptr()))
+    d_filt = torch.empty_like(d_raw)
+    d_rb = torch.empty(nv * m.cg.n_rows * m.cg.n_channels_oversampled, dtype=torch.float32, device="cuda")
+    d_blk = torch.empty(m.rp.nx * m.rp.ny * m.ri.n_slices_block, dtype=torch.float32, device="cuda")
+    taps = (C.c_float * (2 * m.cg.n_channels_oversampled))()
+    L.call("ctbb_load_filter", C.byref(m), taps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev[0].record()
+    L.call("ctbb_adaptive_filter_device", C.byref(m), C.c_void_p(d_raw.data_ptr()), C.c_void_p(d_filt.data_ptr()))
+    ev[1].record()
+    L.call("ctbb_rebin_device", C.byref(m), C.c_void_p(d_filt.data_ptr()), C.c_void_p(d_rb.data_ptr()))
+    ev[2].record()
+    L.call("ctbb_ramp_filter_device", C.c_void_p(d_rb.data_ptr()), nv * m.cg.n_rows, m.cg.n_channels_oversampled, taps)
+    ev[3].record()
+    L.call("ctbb_backproject_device", C.byref(m), C.c_void_p(d_rb.data_ptr()), C.c_void_p(d_blk.data_ptr()))
+    ev[4].record()
+    torch.cuda.synchronize()
+    ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    print(json.dumps({"profile_case": args.config, "block": 0, "n_proj_pull": P, "n_views": nv,
+                      "stage_ms": dict(zip(STAGES[:4], ms)),
+                      "finite": bool(torch.isfinite(d_blk).all().item())}), flush=True)
+    scans.free_plan(mr)
+
+
+def main():
+    args = parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

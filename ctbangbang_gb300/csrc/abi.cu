@@ -23,6 +23,10 @@ namespace ctbb {
 
 namespace {
 
+// Stages timed by ctbb_profile_*: adaptive filter, rebin, ramp filter,
+// backprojection, finalize.
+constexpr int kProfileStages = 5;
+
 // Grow-only device buffer.
 struct DeviceBuffer {
     void *ptr = nullptr;
@@ -64,6 +68,16 @@ struct Context {
     RampFilterPlan ramp;
     void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
     int sms = 0;
+    // host-buffer whole-scan path: second window buffer and a copy stream
+    DeviceBuffer raw_in2;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    // per-stage CUDA-event timing (ctbb_profile_*)
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> open_events[kProfileStages];
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[kProfileStages] = {0};
+    uint64_t stage_launches[kProfileStages] = {0};
 };
 
 Context &ctx()
@@ -71,6 +85,41 @@ Context &ctx()
     static Context *c = new Context;  // never destroyed: no CUDA calls at exit
     return *c;
 }
+
+cudaEvent_t pooled_event(Context &c)
+{
+    if (!c.event_pool.empty()) {
+        cudaEvent_t e = c.event_pool.back();
+        c.event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets the launches of one stage with events on the library stream while
+// profiling is on (the events add no synchronisation).
+struct StageScope {
+    Context &c;
+    int stage;
+    cudaEvent_t start = nullptr;
+    StageScope(Context &cx, int st) : c(cx), stage(st)
+    {
+        if (c.profiling) {
+            start = pooled_event(c);
+            cudaEventRecord(start, c.stream);
+        }
+    }
+    ~StageScope()
+    {
+        if (start) {
+            cudaEvent_t stop = pooled_event(c);
+            cudaEventRecord(stop, c.stream);
+            c.open_events[stage].push_back({start, stop});
+        }
+    }
+};
 
 template <class T>
 int upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t s)
@@ -144,6 +193,7 @@ static int do_adaptive(const struct recon_metadata &mr, const float *d_in, float
     Context &c = ctx();
     size_t n = adaptive_filter_scratch_floats(mr.ri.n_proj_pull);
     CTBB_TRY(c.scratch.ensure(n * sizeof(float)));
+    StageScope scope(c, 0);
     return launch_adaptive_filter(mr, d_in, d_out, c.scratch.as<float>(), c.stream);
 }
 
@@ -153,6 +203,7 @@ static int do_rebin(const struct recon_metadata &mr, const float *d_raw, float *
     RebinTables t;
     CTBB_TRY(build_rebin_tables(mr, &t));
     CTBB_TRY(upload_rebin_tables(t, &c.rebin_tables, c.stream));
+    StageScope scope(c, 1);
     return launch_rebin(t, c.rebin_tables, d_raw, d_rebin, c.stream);
 }
 
@@ -163,6 +214,7 @@ static int do_filter(const struct recon_metadata &mr, float *d_rebin)
     std::vector<float> taps(2 * d.n_os);
     CTBB_TRY(ctbb_load_filter(&mr, taps.data()));
     CTBB_TRY(prepare_ramp_filter(taps.data(), (int)d.n_os, &c.ramp, c.stream));
+    StageScope scope(c, 2);
     return launch_ramp_filter(c.ramp, d_rebin, d.n_views * d.n_rows, c.stream);
 }
 
@@ -173,6 +225,7 @@ static int do_backproject(const struct recon_metadata &mr, const float *d_rebin,
     CTBB_TRY(build_backproject_tables(mr, &t));
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
     CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    StageScope scope(c, 3);
     return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_zpos.as<float>(), d_rebin, d_block,
                               bp_zpt(), c.stream);
 }
@@ -185,6 +238,7 @@ static int do_finalize(const struct recon_metadata &mr, const float *d_image, fl
     CTBB_TRY(upload(c.fin_offsets, t.offsets, c.stream));
     CTBB_TRY(upload(c.fin_slices, t.slices, c.stream));
     CTBB_TRY(upload(c.fin_weights, t.weights, c.stream));
+    StageScope scope(c, 4);
     return launch_finalize(mr, t, c.fin_offsets.as<int>(), c.fin_slices.as<int>(), c.fin_weights.as<float>(),
                            d_image, d_final, mu_water, c.stream);
 }
@@ -492,3 +546,117 @@ int adaptive_filter_kk(struct recon_metadata *mr) { return ctbb_adaptive_filter_
 int rebin_filter(struct recon_metadata *mr) { return ctbb_rebin_filter(mr); }
 int backproject(struct recon_metadata *mr) { return ctbb_backproject(mr); }
 int finalize_image_stack(struct recon_metadata *mr) { return ctbb_finalize_image_stack(mr); }
+
+// --------------------------------------------------------------------------
+// whole scan from host buffers
+// --------------------------------------------------------------------------
+
+extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                                     float mu_water)
+{
+    clear_error();
+    if (!mr || !h_scan || !h_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_host: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.copy_stream) {
+        CTBB_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
+            CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.consumed[i], cudaEventDisableTiming));
+            CTBB_CUDA_TRY(cudaEventRecord(c.consumed[i], c.copy_stream));
+        }
+    }
+    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+    const long long n_readings = mr->rp.n_readings;
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    const size_t n_block = mr->ri.n_slices_block;
+    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+    int n_final = ctbb_n_slices_final(mr);
+    CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
+    DeviceBuffer *win[2] = {&c.raw_in, &c.raw_in2};
+    mr->ri.cb.block_idx = 0;
+    for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
+        struct recon_info ri;
+        CTBB_TRY(plan_next_block(*mr, &ri));
+        mr->ri = ri;
+        BlockDims d = block_dims(*mr);
+        int slot = (int)(b & 1);
+        CTBB_TRY(win[slot]->ensure(d.raw_elems() * sizeof(float)));
+        // H2D of the block's window on the copy stream, once the buffer's
+        // previous reader (the adaptive filter two blocks back) is done
+        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[slot], 0));
+        long long s0 = (long long)(int)mr->ri.idx_pull_start, s1 = s0 + (long long)d.n_proj_pull;
+        long long a = s0 < 0 ? 0 : s0, e = s1 > n_readings ? n_readings : s1;
+        float *dst = win[slot]->as<float>();
+        if (a > s0) CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(a - s0) * frame * sizeof(float), c.copy_stream));
+        if (e < s1) {
+            long long z0 = e > s0 ? e : s0;
+            CTBB_CUDA_TRY(cudaMemsetAsync(dst + (size_t)(z0 - s0) * frame, 0, (size_t)(s1 - z0) * frame * sizeof(float),
+                                          c.copy_stream));
+        }
+        if (e > a)
+            CTBB_CUDA_TRY(cudaMemcpyAsync(dst + (size_t)(a - s0) * frame, h_scan + (size_t)a * frame,
+                                          (size_t)(e - a) * frame * sizeof(float), cudaMemcpyHostToDevice,
+                                          c.copy_stream));
+        CTBB_CUDA_TRY(cudaEventRecord(c.copied[slot], c.copy_stream));
+        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copied[slot], 0));
+        CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
+        CTBB_TRY(do_adaptive(*mr, dst, c.raw_filt.as<float>()));
+        CTBB_CUDA_TRY(cudaEventRecord(c.consumed[slot], c.stream));
+        CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
+        CTBB_TRY(do_rebin(*mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+        CTBB_TRY(do_filter(*mr, c.rebin.as<float>()));
+        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>(), c.image.as<float>() + b * n_block * plane));
+    }
+    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
+                                  cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
+// --------------------------------------------------------------------------
+// per-stage timing
+// --------------------------------------------------------------------------
+
+extern "C" int ctbb_profile_enable(int on)
+{
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.profiling = on != 0;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_profile_read(double *ms, uint64_t *launches, int n, int reset)
+{
+    clear_error();
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (int s = 0; s < kProfileStages; ++s) {
+        for (auto &ev : c.open_events[s]) {
+            CTBB_CUDA_TRY(cudaEventSynchronize(ev.second));
+            float t = 0.0f;
+            CTBB_CUDA_TRY(cudaEventElapsedTime(&t, ev.first, ev.second));
+            c.stage_ms[s] += t;
+            c.stage_launches[s] += 1;
+            c.event_pool.push_back(ev.first);
+            c.event_pool.push_back(ev.second);
+        }
+        c.open_events[s].clear();
+    }
+    for (int s = 0; s < n && s < kProfileStages; ++s) {
+        if (ms) ms[s] = c.stage_ms[s];
+        if (launches) launches[s] = c.stage_launches[s];
+    }
+    if (reset)
+        for (int s = 0; s < kProfileStages; ++s) {
+            c.stage_ms[s] = 0.0;
+            c.stage_launches[s] = 0;
+        }
+    return kProfileStages;
+}

@@ -13,7 +13,11 @@
 //
 // interp2 (src/interp.cu:29-64) returns 0 when p_idx or q_idx leaves
 // [0, dim - 2]; the weight W is still added to h in that case, and this kernel
-// keeps that rule.  The reference's pi' = 3.1415368979f is used where it uses it.
+// keeps that rule.  Both borders are jumps in the result, so the quantities
+// that decide them (voxel centre, p, p_idx, and near the border q_idx) are
+// evaluated with the reference's float operations; the smooth parts (weights,
+// interpolation) use FMA and reciprocals.  The reference's pi' = 3.1415368979f
+// is used where it uses it.
 //
 // GB300 mapping: one thread per (x, y) column and ZPT consecutive slices; the
 // per-(x, y, view) geometry (asin, sqrt, reciprocal) is computed once and
@@ -40,9 +44,10 @@ struct BpParams {
     const float *zpos;     // [n_slices_block]
     int nx, ny, n_slices, nos, n_rows, nht, n_half;
     float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
-    float inv_ds_half;     // 1 / (r_f fai / 2)
+    float ds_half;         // r_f fai / 2
     float two_cc;          // 2 * central channel
-    float inv_rf, rf2;
+    float rf, inv_rf, rf2; // r_f, 1 / r_f, r_f^2
+    float z_rot, two_pi;   // z_rot, 2 pi'
     float zrot_over_2pi;
     float tan_cone;
     float half_rows;       // (R - 1) / 2
@@ -52,6 +57,27 @@ struct BpParams {
 
 constexpr float kQ = 0.6f;
 
+// interp2 drops a sample when q_idx > R*nht - 2, which only the last half
+// turn can reach.  Its weight still counts, so the decision is a jump in the
+// image; near it the reference's own float q_idx decides.  This recomputes that
+// q_idx with the reference's operations and rounding (asin through double,
+// i.e. correctly rounded); it runs only when the fast coordinate is within
+// kBorderBand rows of the border.
+__device__ __forceinline__ bool last_turn_sample_valid(const BpParams &p, float x, float y, float theta,
+                                                    float s, float c, float phat, float z, int k)
+{
+    float asn = (float)asin((double)__fdiv_rn(phat, p.rf));
+    float ray = __fdiv_rn(__fmul_rn(p.z_rot, __fsub_rn(theta, asn)), p.two_pi);
+    float lhat = __fsub_rn(__fsub_rn(__fsqrt_rn(__fsub_rn(p.rf2, __fmul_rn(phat, phat))), __fmul_rn(x, c)),
+                           __fmul_rn(y, s));
+    float qhat = __fdiv_rn(__fsub_rn(z, ray), __fmul_rn(lhat, p.tan_cone));
+    float q_idx = __fadd_rn(__fmul_rn(__fdiv_rn(__fadd_rn(qhat, 1.0f), 2.0f), (float)p.n_rows - 1.0f),
+                            (float)(k * p.n_rows));
+    return !(q_idx > (float)(p.n_rows * p.nht - 2)) && !(q_idx < 0.0f);
+}
+
+constexpr float kBorderBand = 1e-3f;
+
 template <int ZPT>
 __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
 {
@@ -59,8 +85,9 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
     int yi = blockIdx.y * blockDim.y + threadIdx.y;
     int z0 = blockIdx.z * ZPT;
     if (xi >= p.nx || yi >= p.ny) return;
-    float x = p.pix_x * ((float)xi - p.x_c) + p.x0;
-    float y = p.pix_y * ((float)yi - p.y_c) + p.y0;
+    // voxel centre with the reference's float operations (no contraction)
+    float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
+    float y = __fadd_rn(__fmul_rn(p.pix_y, __fsub_rn((float)yi, p.y_c)), p.y0);
 
     float zp[ZPT], img[ZPT];
 #pragma unroll
@@ -81,14 +108,16 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
         }
         for (int k = 0; k < p.nht; ++k) {
             float4 t = __ldg(p.views + (size_t)i * p.nht + k);
-            float phat = x * t.y - y * t.z;
-            float p_idx = phat * p.inv_ds_half + p.two_cc;
+            // p and its detector index exactly as the reference rounds them: the
+            // p border of interp2 is then decided identically
+            float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
+            float p_idx = __fadd_rn(__fdiv_rn(phat, p.ds_half), p.two_cc);
             bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
             float ray = (t.x - asinf(phat * p.inv_rf)) * p.zrot_over_2pi;
             float lhat = sqrtf(p.rf2 - phat * phat) - x * t.z - y * t.y;
             float inv_den = 1.0f / (lhat * p.tan_cone);
             float q_off = -ray * inv_den;
-            float q_lim = (k == p.nht - 1) ? q_max_last : 3.0e38f;
+            bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
             const float *view = p.rebin + ((size_t)i + (size_t)k * p.n_half) * view_stride + ip;
@@ -104,8 +133,17 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
                     }
                     h[z] += w;
                     float ql = (q + 1.0f) * p.half_rows;
-                    if (p_ok && ql <= q_lim) {
-                        int iq = (int)ql;
+                    bool ok = p_ok;
+                    if (ok && last) {
+                        float dq = ql - q_max_last;
+                        if (dq > kBorderBand) ok = false;
+                        else if (dq > -kBorderBand)
+                            ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, zp[z], k);
+                    }
+                    if (ok) {
+                        // (q + 1) (R - 1) / 2 can round up to R - 1 for q just below 1:
+                        // keep the second row inside the view
+                        int iq = min((int)ql, p.n_rows - 2);
                         float wq = ql - (float)iq;
                         const float *r0 = view + (size_t)iq * p.nos;
                         float v00 = __ldg(r0), v01 = __ldg(r0 + 1);
@@ -186,10 +224,13 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     p.y_c = (float)(rp.ny - 1) / 2.0f;
     p.x0 = rp.x_origin;
     p.y0 = rp.y_origin;
-    p.inv_ds_half = 1.0f / (cg.r_f * cg.fan_angle_increment / 2.0f);
+    p.ds_half = cg.r_f * cg.fan_angle_increment / 2.0f;
     p.two_cc = 2.0f * cg.central_channel;
+    p.rf = cg.r_f;
     p.inv_rf = 1.0f / cg.r_f;
-    p.rf2 = cg.r_f * cg.r_f;
+    p.rf2 = std::pow(cg.r_f, 2.0f);
+    p.z_rot = cg.z_rot;
+    p.two_pi = 2.0f * pi;
     p.zrot_over_2pi = cg.z_rot / (2.0f * pi);
     p.tan_cone = std::tan(cg.theta_cone / 2.0f);
     p.half_rows = ((float)cg.n_rows - 1.0f) / 2.0f;

@@ -129,15 +129,17 @@ CONFIGS = {
 
 def tiny(z_ffs=0, phi_ffs=0, *, n_channels=64, n_rows_raw=4, nx=32, ny=32, n_slices=8,
          seed=7, adaptive_filtration=0.0, turns=None, reverse_row_interleave=0,
-         table_dir="out", start_pos=None, slice_thickness=None, n_proj_turn=96, i0=1e5):
-    """A small scan of any FFS mode (64 channels, 96 views/turn, 32^2 pixels)."""
+         table_dir="out", start_pos=None, slice_thickness=None, n_proj_turn=96, i0=1e5,
+         fan_angle_increment=None, recon_kernel=-100, pitch=1.0):
+    """A small scan of any FFS mode (default 64 channels, 96 views/turn, 32^2 pixels)."""
+    fai = fan_angle_increment if fan_angle_increment is not None else 0.48 / n_channels
     n_rows = n_rows_raw * 2 ** z_ffs
     coll = 1.0
     st = slice_thickness if slice_thickness is not None else coll
     spec = ScanSpec(
         name="tiny_z%d_p%d" % (z_ffs, phi_ffs), r_f=300.0, src_to_det=550.0, anode_angle=0.1222,
-        fan_angle_increment=0.0075, central_channel=(n_channels / 2) - 0.75,
-        n_proj_turn=n_proj_turn, n_channels=n_channels, n_rows=n_rows, coll=coll, pitch=2.0,
+        fan_angle_increment=fai, central_channel=(n_channels / 2) - 0.75, recon_kernel=recon_kernel,
+        n_proj_turn=n_proj_turn, n_channels=n_channels, n_rows=n_rows, coll=coll, pitch=pitch,
         turns=1.0, slice_thickness=st, recon_fov=100.0, nx=nx, ny=ny, start_pos=start_pos,
         n_slices=n_slices, z_ffs=z_ffs, phi_ffs=phi_ffs, adaptive_filtration=adaptive_filtration,
         reverse_row_interleave=reverse_row_interleave, table_dir=table_dir, seed=seed,

@@ -187,6 +187,13 @@ const char *ctbb_last_error(void);
 /* Library version string. */
 const char *ctbb_version(void);
 
+/* sizeof(struct recon_metadata) followed by the offsets of its members flags,
+   rp, ri, cg, ctd, tube_angles, table_positions and of recon_params.nx,
+   recon_params.table_dir, recon_info.cb, ct_geom.table_direction, as compiled
+   into the library (a binding checks its own struct mirror against these).
+   Writes min(n, 12) values; returns 12. */
+int ctbb_struct_layout(size_t *out, int n);
+
 /* Stream on which all device work of the following calls is issued
    (a cudaStream_t passed as void*; NULL = legacy default stream). */
 int ctbb_set_stream(void *stream);
@@ -311,6 +318,25 @@ int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image,
    library between calls. */
 int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
                             float *d_final, float mu_water);
+
+/* As ctbb_reconstruct_device from host buffers: each block's pull window is
+   copied from h_scan [n_readings][n_rows_raw][n_channels] on a second stream
+   (double-buffered, overlapping the previous block's compute when h_scan is
+   pinned) and the final stack is copied to h_final [n_slices_final][ny][nx]. */
+int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                          float mu_water);
+
+/* Per-stage device timing with CUDA events on the library stream.
+   Stages: 0 adaptive filter, 1 rebin, 2 ramp filter, 3 backprojection,
+   4 finalize.  ctbb_profile_read synchronises on the recorded events, adds
+   their durations to per-stage totals, writes min(n, 5) totals (ms) and launch
+   counts, optionally resets them, and returns 5. */
+int ctbb_profile_enable(int on);
+int ctbb_profile_read(double *ms, uint64_t *launches, int n, int reset);
+
+/* Measured FP32 FMA throughput of the current device (best of `repeats`
+   launches of a register-only FMA loop), TFLOP/s; -1 without a device. */
+double ctbb_fp32_peak_tflops(int repeats);
 
 /* Bytes of device workspace ctbb_reconstruct_device keeps for this plan. */
 size_t ctbb_workspace_bytes(const struct recon_metadata *mr);

@@ -1,0 +1,188 @@
+"""CPU tests of the boundary: struct layout, exported symbols, the host
+planner against the reference planner's golden tables, the .prm parser, the
+ramp-kernel generator against the reference's kernel files, and the loud
+failure of compute entry points without a GPU."""
+import ctypes as C
+import glob
+import hashlib
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ctbangbang_gb300 import lib as L
+from ctbangbang_gb300 import scans, structs
+from tests.conftest import HAS_GPU, REPO
+
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def test_struct_layout_matches_header(lib):
+    arr = (C.c_size_t * 12)()
+    n = lib.ctbb_struct_layout(arr, 12)
+    assert n == 12
+    assert arr[0] == C.sizeof(structs.ReconMetadata)
+    assert list(arr)[1:] == structs.layout_offsets()
+
+
+def test_struct_layout_matches_reference(lib, ref_lib):
+    assert ref_lib.ref_sizeof_recon_metadata() == C.sizeof(structs.ReconMetadata)
+    assert [ref_lib.ref_offsetof(i) for i in range(11)] == structs.layout_offsets()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    header = open(os.path.join(REPO, "include", "ctbb_gb300.h")).read()
+    declared = set(re.findall(r"^(?:const\s+)?[a-z_0-9]+\s*\*?\s*(ctbb_[a-z0-9_]+)\s*\(", header, re.M))
+    assert len(declared) >= 29
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python prototypes cover every declared entry point
+    assert declared <= set(L.PROTOTYPES) | {"ctbb_struct_layout"}
+    # the C++-linkage drop-ins of the reference signatures
+    out = os.popen("nm -D --defined-only %s" % L.LIB_PATH).read()
+    for mangled in ("_Z18adaptive_filter_kkP14recon_metadata", "_Z12rebin_filterP14recon_metadata",
+                    "_Z11backprojectP14recon_metadata", "_Z20finalize_image_stackP14recon_metadata"):
+        assert mangled in out
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.ctbb_version()
+
+
+@pytest.mark.skipif(HAS_GPU, reason="checks the no-device error path")
+def test_compute_entry_points_fail_loudly_without_gpu(lib, tmp_path):
+    spec = scans.tiny(0, 0)
+    mr = scans.plan_spec(spec, str(tmp_path))
+    lib.ctbb_update_block_info(C.byref(mr))
+    for name in ("ctbb_adaptive_filter_kk", "ctbb_rebin_filter", "ctbb_finalize_image_stack"):
+        st = getattr(lib, name)(C.byref(mr))
+        assert L.STATUS[st] == "CTBB_ERR_NO_DEVICE", name
+        assert b"no CUDA device" in lib.ctbb_last_error()
+    with pytest.raises(L.CtbbError):
+        L.call("ctbb_rebin_filter", C.byref(mr))
+    scans.free_plan(mr)
+
+
+# ---------------------------------------------------------------- planner
+
+def _plan_fixtures():
+    return sorted(glob.glob(os.path.join(GOLDEN, "plan_*.json")))
+
+
+def _ri(mr):
+    ri = {f: getattr(mr.ri, f) for f, _ in structs.ReconInfo._fields_ if f != "cb"}
+    ri.update({"cb." + f: getattr(mr.ri.cb, f) for f, _ in structs.BlockInfo._fields_})
+    return ri
+
+
+def _spec_from(d):
+    keep = {k: v for k, v in d.items() if k in scans.ScanSpec.__dataclass_fields__}
+    return scans.ScanSpec(**keep)
+
+
+@pytest.mark.parametrize("path", _plan_fixtures(), ids=lambda p: os.path.basename(p))
+def test_planner_bit_exact_vs_reference_golden(lib, tmp_path, path):
+    """configure_ct_geom / configure_reconstruction / update_block_info of this
+    library reproduce the reference planner's integers and float tables exactly."""
+    fx = json.load(open(path))
+    spec = _spec_from(fx["spec"])
+    mr = scans.plan_spec(spec, str(tmp_path))
+    n = spec.n_readings
+    for k, v in fx["geom"].items():
+        assert getattr(mr.cg, k) == pytest.approx(v, abs=0) or np.float32(getattr(mr.cg, k)) == np.float32(v), k
+    assert np.float32(mr.rp.end_pos) == np.float32(fx["rp_end_pos"])
+    got = _ri(mr)
+    for k, v in fx["plan"].items():
+        assert np.float32(got[k]) == np.float32(v) if isinstance(v, float) else got[k] == v, k
+    assert hashlib.sha256(C.string_at(mr.tube_angles, 4 * n)).hexdigest() == fx["tube_angles_sha256"]
+    assert hashlib.sha256(C.string_at(mr.table_positions, 8 * n)).hexdigest() == fx["table_positions_sha256"]
+    assert len(fx["blocks"]) == mr.ri.n_blocks
+    for blk in fx["blocks"]:
+        lib.ctbb_update_block_info(C.byref(mr))
+        got = _ri(mr)
+        for k, v in blk.items():
+            assert np.float32(got[k]) == np.float32(v) if isinstance(v, float) else got[k] == v, (k, got[k], v)
+    scans.free_plan(mr)
+
+
+def test_planner_rejects_out_of_range(lib, tmp_path):
+    spec = scans.tiny(0, 0)
+    spec.start_pos = -50.0
+    prm, inst = scans.prepare(spec, str(tmp_path))
+    with pytest.raises(L.CtbbError) as e:
+        scans.plan(prm, inst)
+    assert e.value.status_name == "CTBB_ERR_RANGE"
+
+
+def test_prm_missing_key_is_an_error_not_exit(lib, tmp_path):
+    p = tmp_path / "bad.prm"
+    p.write_text("Nrows:\t16\n% no CollSlicewidth\n")
+    rp = structs.ReconParams()
+    st = lib.ctbb_configure_recon_params(str(p).encode(), C.byref(rp))
+    assert L.STATUS[st] == "CTBB_ERR_CONFIG"
+    assert rp.n_rows == 16
+
+
+def test_prm_parser_matches_reference(lib, ref_lib, tmp_path):
+    spec = scans.CONFIGS["config2"]
+    prm, _ = scans.prepare(spec, str(tmp_path))
+    with open(prm, "a") as f:
+        f.write("TableFeed:\t12.5 % overrides PitchValue\nNSlices:\t7\n")
+    a, b = structs.ReconParams(), structs.ReconParams()
+    L.call("ctbb_configure_recon_params", prm.encode(), C.byref(a))
+    ref_lib.ref_configure_recon_params(prm.encode(), C.byref(b))
+    assert bytes(a) == bytes(b)
+
+
+def test_builtin_scanners_match_reference(lib, ref_lib, tmp_path):
+    for scanner in ("0", "1", "2"):
+        spec = scans.CONFIGS["config2"]
+        prm, inst = scans.prepare(spec, str(tmp_path))
+        mr_a, mr_b = structs.ReconMetadata(), structs.ReconMetadata()
+        for mr in (mr_a, mr_b):
+            L.call("ctbb_configure_recon_params", prm.encode(), C.byref(mr.rp))
+            mr.rp.scanner = scanner.encode()
+            mr.install_dir = inst.encode()
+        L.call("ctbb_configure_ct_geom", C.byref(mr_a))
+        ref_lib.ref_configure_ct_geom(C.byref(mr_b))
+        assert bytes(mr_a.cg) == bytes(mr_b.cg), scanner
+        assert mr_a.rp.file_subtype == mr_b.rp.file_subtype
+
+
+# ---------------------------------------------------------------- filter taps
+
+def test_ramp_taps_equal_reference_sharp_kernels(lib):
+    """KAT: the reference's f_<N>_sharp files are the ramp formula of
+    resources/ramp.m with c = 1, a = 1, ds = r_f sin(fai/2)."""
+    kat = json.load(open(os.path.join(GOLDEN, "ramp_kat.json")))
+    geo = {"f_736_sharp": (595.0, 0.067864 * 3.1415926535897 / 180.0),   # Definition AS
+           "f_672_sharp": (570.0, 0.07758621 * 3.1415926535897 / 180.0)}  # Sensation 64
+    for name, fx in kat.items():
+        r_f, fai = geo[name]
+        n_os = fx["n_os"]
+        taps = (C.c_float * (2 * n_os))()
+        ds = np.float32(r_f * np.sin(np.float32(fai) / 2.0))
+        L.call("ctbb_ramp_filter_taps", n_os, C.c_float(float(ds)), 1.0, 1.0, taps)
+        t = np.frombuffer(taps, np.float32)
+        np.testing.assert_allclose(t[n_os - 8:n_os + 9], fx["centre_taps"], rtol=0, atol=2e-7)
+        assert abs(t.astype(np.float64).sum() - fx["sum"]) < 1e-5
+
+
+def test_load_filter_generates_missing_ramp(lib, tmp_path):
+    spec = scans.tiny(0, 0)
+    mr = scans.plan_spec(spec, str(tmp_path))
+    for f in glob.glob(str(tmp_path / "resources" / "filters" / "*")):
+        os.remove(f)
+    n = 2 * mr.cg.n_channels_oversampled
+    t = (C.c_float * n)()
+    L.call("ctbb_load_filter", C.byref(mr), t)
+    taps = np.frombuffer(t, np.float32)
+    ds = mr.cg.r_f * np.sin(mr.cg.fan_angle_increment / 2.0)
+    assert taps[n // 2] == pytest.approx(1.0 / (4.0 * ds), rel=1e-6)
+    mr.rp.recon_kernel = 2  # "medium" is not present: a clear error, not exit()
+    with pytest.raises(L.CtbbError) as e:
+        L.call("ctbb_load_filter", C.byref(mr), t)
+    assert e.value.status_name == "CTBB_ERR_IO"
+    scans.free_plan(mr)

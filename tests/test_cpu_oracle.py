@@ -1,0 +1,133 @@
+"""CPU tests pinning the oracle restatement: against the golden fixtures the
+reference's own CPU code produced, and (where the reference build is present)
+against that build directly on fresh inputs."""
+import ctypes as C
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from ctbangbang_gb300 import lib as L
+from ctbangbang_gb300 import scans
+from tests import helpers as H
+from tests.conftest import REPO
+
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def assert_rebin_matches_golden(got, golden):
+    """Unfiltered rebin vs the golden made through a unit-impulse kernel: that
+    pass is exact except on samples that were exactly 0 (frames past the end
+    of the data), where the reference's double FFT leaves ~1e-16 of roundoff."""
+    zero = np.abs(golden) < 1e-9
+    np.testing.assert_array_equal(got[~zero], golden[~zero])
+    assert np.all(np.abs(got[zero]) < 1e-9)
+
+
+def golden_block_files():
+    return sorted(glob.glob(os.path.join(GOLDEN, "block_*.npz")))
+
+
+def load_case(path):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    import synth
+    z = np.load(path)
+    meta = json.loads(bytes(z["meta"]).decode())
+    keep = {k: v for k, v in meta["spec"].items() if k in scans.ScanSpec.__dataclass_fields__}
+    spec = scans.ScanSpec(**keep)
+    frames = make_golden.synth_frames(spec)
+    assert synth.sha256(frames) == meta["frames_sha256"], "synthetic input not reproduced bit for bit"
+    return z, meta, spec, frames
+
+
+class GoldenScan(H.Scan):
+    """H.Scan whose frames are the golden synthetic input."""
+
+    def __init__(self, spec, frames, workdir):
+        self.spec = spec
+        self._tmp = None
+        self.workdir = workdir
+        self.prm, self.install = scans.prepare(spec, workdir)
+        self.mr = scans.plan(self.prm, self.install)
+        self.frames = frames
+
+
+@pytest.mark.parametrize("path", golden_block_files(), ids=lambda p: os.path.basename(p)[6:-4])
+def test_oracle_matches_reference_golden(lib, oracle_lib, tmp_path, path):
+    z, meta, spec, frames = load_case(path)
+    scan = GoldenScan(spec, frames, str(tmp_path))
+    step = meta["view_step"]
+    mr = scan.mr
+    for b in range(meta["n_blocks"]):
+        raw = scan.next_block()
+        d = H.dims(mr)
+        import synth
+        assert synth.sha256(raw) == bytes(z["raw_sha256_b%d" % b]).decode()
+        st = H.oracle_block(oracle_lib, scan, raw, adaptive=True)
+        changed = np.nonzero(st["adaptive"] != raw)[0]
+        np.testing.assert_array_equal(changed, z["adaptive_idx_b%d" % b])
+        np.testing.assert_array_equal(st["adaptive"][changed], z["adaptive_val_b%d" % b])
+        vs = mr.cg.n_rows * mr.cg.n_channels_oversampled
+        assert_rebin_matches_golden(st["rebin"].reshape(-1, vs)[::step], z["rebin_b%d" % b])
+        np.testing.assert_array_equal(st["filtered"].reshape(-1, vs)[::step], z["filtered_b%d" % b])
+    np.testing.assert_array_equal(H.view(mr.ctd.image, d["n_image"]), z["image"])
+    oracle_lib.oracle_finalize(C.byref(mr))
+    n_final = L.load().ctbb_n_slices_final(C.byref(mr))
+    assert n_final == meta["n_final"]
+    np.testing.assert_array_equal(H.view(mr.ctd.final_image_stack, n_final * d["plane"]), z["final"])
+    scan.close()
+
+
+@pytest.mark.parametrize("z_ffs,phi_ffs", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_oracle_bit_exact_vs_reference_build(lib, oracle_lib, ref_lib, tmp_path, z_ffs, phi_ffs):
+    """Fresh phantom scans through the reference's own CPU functions and the
+    oracle: every stage identical."""
+    spec = scans.tiny(z_ffs, phi_ffs, adaptive_filtration=3.0, seed=100 + 2 * z_ffs + phi_ffs)
+    scan = H.Scan(spec, str(tmp_path))
+    from ctbangbang_gb300 import structs
+    mref = structs.ReconMetadata()
+    ref_lib.ref_configure_recon_params(scan.prm.encode(), C.byref(mref.rp))
+    mref.install_dir = scan.install.encode()
+    ref_lib.ref_configure_ct_geom(C.byref(mref))
+    ref_lib.ref_configure_reconstruction(C.byref(mref))
+    mr = scan.mr
+    for _ in range(mr.ri.n_blocks):
+        raw = scan.next_block()
+        ref_lib.ref_update_block_info(C.byref(mref))
+        ref_lib.ref_extract_projections(C.byref(mref))
+        d = H.dims(mr)
+        np.testing.assert_array_equal(H.view(mref.ctd.raw, d["n_raw"]), raw)
+        ref_lib.ref_adaptive_filter_kk(C.byref(mref))
+        oracle_lib.oracle_adaptive_filter(C.byref(mr))
+        np.testing.assert_array_equal(H.view(mr.ctd.raw, d["n_raw"]), H.view(mref.ctd.raw, d["n_raw"]))
+        ref_lib.ref_rebin_filter_cpu(C.byref(mref))
+        assert oracle_lib.oracle_rebin_filter(C.byref(mr)) == 0
+        np.testing.assert_array_equal(H.view(mr.ctd.rebin, d["n_rebin"]), H.view(mref.ctd.rebin, d["n_rebin"]))
+        ref_lib.ref_backproject_cpu(C.byref(mref))
+        oracle_lib.oracle_backproject(C.byref(mr))
+        np.testing.assert_array_equal(H.view(mr.ctd.image, d["n_image"]), H.view(mref.ctd.image, d["n_image"]))
+    ref_lib.ref_finalize_image_stack_cpu(C.byref(mref))
+    oracle_lib.oracle_finalize(C.byref(mr))
+    nf = L.load().ctbb_n_slices_final(C.byref(mr)) * d["plane"]
+    np.testing.assert_array_equal(H.view(mr.ctd.final_image_stack, nf), H.view(mref.ctd.final_image_stack, nf))
+    ref_lib.ref_free(C.byref(mref))
+    scan.close()
+
+
+def test_interp_edge_rules_match_reference(oracle_lib, ref_lib):
+    """interp2 border (value 0 beyond [0, dim-2]) and interp3 clamping/aliasing."""
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal(6 * 5 * 4).astype(np.float32)
+    p = a.ctypes.data_as(C.POINTER(C.c_float))
+    pts = [-1.0, -0.0, 0.0, 0.25, 3.0, 3.5, 4.0, 4.0001, 5.0, 6.0]
+    for i1 in pts:
+        for i2 in pts:
+            assert oracle_lib.oracle_interp2(p, 6, 5, i1, i2) == ref_lib.ref_interp2(p, 6, 5, i1, i2)
+            for i3 in (-2.0, 0.0, 1.5, 3.0, 3.25, 9.0):
+                x = oracle_lib.oracle_interp3(p, 6, 5, 4, i1, i2, i3)
+                y = ref_lib.ref_interp3(p, 6, 5, 4, i1, i2, i3)
+                assert x == y or (np.isnan(x) and np.isnan(y))

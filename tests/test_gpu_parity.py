@@ -1,0 +1,256 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the
+oracle (the reference CPU path's arithmetic) and the reference's golden
+fixtures.
+
+Bars (float32 image work in HU, 1 HU = 0.019/1000 per mm):
+  adaptive filter, unfiltered rebin, finalize:  bit-exact
+  ramp filter (FP32 FFT vs the reference's double FFT): |err| <= 2e-5 * max|row|
+  backprojection / end to end:                   <= 1 HU max, <= 0.1 HU RMS
+  device whole-scan path vs drop-in calls:       bit-exact
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from ctbangbang_gb300 import lib as L
+from ctbangbang_gb300 import scans
+from tests import helpers as H
+from tests.test_cpu_oracle import GoldenScan, assert_rebin_matches_golden, golden_block_files, load_case
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(0, 0), (0, 1), (1, 0), (1, 1)]
+FILTER_RTOL = 2e-5
+HU_MAX, HU_RMS = 1.0, 0.1
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def assert_filter_close(got, want):
+    scale = float(np.abs(want).max())
+    err = float(np.abs(got.astype(np.float64) - want).max())
+    assert err <= FILTER_RTOL * scale, (err, scale)
+
+
+def assert_hu(got, want):
+    mx, rms = H.hu_errors(got, want)
+    assert mx <= HU_MAX and rms <= HU_RMS, (mx, rms)
+    return mx, rms
+
+
+@pytest.fixture(params=MODES, ids=lambda m: "z%d_p%d" % m)
+def mode_scan(request, lib, tmp_path):
+    z, p = request.param
+    spec = scans.tiny(z, p, adaptive_filtration=3.0, seed=200 + 2 * z + p)
+    s = H.Scan(spec, str(tmp_path))
+    yield s
+    s.close()
+
+
+def test_adaptive_filter_bit_exact(torch_cuda, oracle_lib, mode_scan):
+    mr = mode_scan.mr
+    raw = mode_scan.next_block()
+    want = H.oracle_block(oracle_lib, mode_scan, raw)["adaptive"]
+    assert (want != raw).sum() > 0
+    L.call("ctbb_adaptive_filter_kk", C.byref(mr))
+    got = H.view(mr.ctd.raw, H.dims(mr)["n_raw"]).copy()
+    np.testing.assert_array_equal(got, want)
+
+
+def test_rebin_bit_exact_and_filter(torch_cuda, oracle_lib, mode_scan):
+    torch = torch_cuda
+    mr = mode_scan.mr
+    raw = mode_scan.next_block()
+    st = H.oracle_block(oracle_lib, mode_scan, raw)
+    d = H.dims(mr)
+    d_raw = dev(torch, st["adaptive"])
+    d_rb = torch.empty(d["n_rebin"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_rebin_device", C.byref(mr), ptr(d_raw), ptr(d_rb))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d_rb.cpu().numpy(), st["rebin"])
+    taps = H.taps_of(mr)
+    L.call("ctbb_ramp_filter_device", ptr(d_rb), d["n_views"] * mr.cg.n_rows, mr.cg.n_channels_oversampled, fptr(taps))
+    torch.cuda.synchronize()
+    assert_filter_close(d_rb.cpu().numpy(), st["filtered"])
+
+
+def test_backproject_hu(torch_cuda, oracle_lib, mode_scan):
+    torch = torch_cuda
+    mr = mode_scan.mr
+    raw = mode_scan.next_block()
+    st = H.oracle_block(oracle_lib, mode_scan, raw)
+    d = H.dims(mr)
+    d_rb = dev(torch, st["filtered"])
+    d_blk = torch.empty(d["n_block"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_backproject_device", C.byref(mr), ptr(d_rb), ptr(d_blk))
+    torch.cuda.synchronize()
+    assert_hu(d_blk.cpu().numpy(), st["block"])
+
+
+def run_dropin(scan):
+    """main.cu's block loop and finalize through the drop-in entry points."""
+    mr = scan.mr
+    for _ in range(mr.ri.n_blocks):
+        scan.next_block()
+        L.call("ctbb_adaptive_filter_kk", C.byref(mr))
+        L.call("ctbb_rebin_filter", C.byref(mr))
+        L.call("ctbb_backproject", C.byref(mr))
+    L.call("ctbb_finalize_image_stack", C.byref(mr))
+    d = H.dims(mr)
+    n_final = L.load().ctbb_n_slices_final(C.byref(mr))
+    img = H.view(mr.ctd.image, d["n_image"]).copy()
+    fin = H.view(mr.ctd.final_image_stack, n_final * d["plane"]).copy()
+    return img, fin
+
+
+def run_oracle(orc, scan):
+    mr = scan.mr
+    for _ in range(mr.ri.n_blocks):
+        raw = scan.next_block()
+        scan.set_raw(raw)
+        orc.oracle_adaptive_filter(C.byref(mr))
+        orc.oracle_rebin_filter(C.byref(mr))
+        orc.oracle_backproject(C.byref(mr))
+    orc.oracle_finalize(C.byref(mr))
+    d = H.dims(mr)
+    n_final = L.load().ctbb_n_slices_final(C.byref(mr))
+    return (H.view(mr.ctd.image, d["n_image"]).copy(),
+            H.view(mr.ctd.final_image_stack, n_final * d["plane"]).copy())
+
+
+def reset_blocks(scan):
+    scan.mr.ri.cb.block_idx = 0
+
+
+@pytest.mark.parametrize("variant", ["multi_block_in", "reverse_rows", "strength0"])
+def test_dropin_pipeline_vs_oracle(torch_cuda, oracle_lib, lib, tmp_path, variant):
+    if variant == "multi_block_in":
+        spec = scans.tiny(0, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, table_dir="in", seed=31)
+    elif variant == "reverse_rows":
+        spec = scans.tiny(1, 1, adaptive_filtration=2.0, reverse_row_interleave=1, seed=32)
+    else:
+        spec = scans.tiny(1, 0, adaptive_filtration=0.0, seed=33)
+    scan = H.Scan(spec, str(tmp_path))
+    img_g, fin_g = run_dropin(scan)
+    reset_blocks(scan)
+    scan.mr.ctd.final_image_stack = None  # the drop-in's stack stays allocated (test only)
+    img_o, fin_o = run_oracle(oracle_lib, scan)
+    assert_hu(img_g, img_o)
+    assert_hu(fin_g, fin_o)
+    # finalize alone is bit-exact given the same image
+    H.view(scan.mr.ctd.image, img_o.size)[:] = img_o
+    L.call("ctbb_finalize_image_stack", C.byref(scan.mr))
+    np.testing.assert_array_equal(H.view(scan.mr.ctd.final_image_stack, fin_o.size), fin_o)
+    scan.close()
+
+
+def test_reconstruct_device_equals_dropin(torch_cuda, lib, tmp_path):
+    torch = torch_cuda
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=41)
+    scan = H.Scan(spec, str(tmp_path))
+    _, fin_g = run_dropin(scan)
+    d_scan = dev(torch, scan.frames.reshape(-1))
+    d_fin = torch.empty(fin_g.size, dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_device", C.byref(scan.mr), ptr(d_scan), ptr(d_fin), 0.0)
+    np.testing.assert_array_equal(d_fin.cpu().numpy(), fin_g)
+    # HU output: 1000 (mu - mu_w) / mu_w of the same stack
+    L.call("ctbb_reconstruct_device", C.byref(scan.mr), ptr(d_scan), ptr(d_fin), scans.MU_WATER)
+    hu = d_fin.cpu().numpy()
+    np.testing.assert_allclose(hu, 1000.0 * (fin_g - scans.MU_WATER) / scans.MU_WATER, rtol=1e-5, atol=1e-3)
+    scan.close()
+
+
+@pytest.mark.parametrize("path", golden_block_files(), ids=lambda p: os.path.basename(p)[6:-4])
+def test_gpu_vs_reference_golden(torch_cuda, lib, tmp_path, path):
+    """The CUDA path against outputs of the reference's own CPU code."""
+    torch = torch_cuda
+    z, meta, spec, frames = load_case(path)
+    scan = GoldenScan(spec, frames, str(tmp_path))
+    mr = scan.mr
+    step = meta["view_step"]
+    for b in range(meta["n_blocks"]):
+        raw = scan.next_block()
+        d = H.dims(mr)
+        L.call("ctbb_adaptive_filter_kk", C.byref(mr))
+        got = H.view(mr.ctd.raw, d["n_raw"]).copy()
+        changed = np.nonzero(got != raw)[0]
+        np.testing.assert_array_equal(changed, z["adaptive_idx_b%d" % b])
+        np.testing.assert_array_equal(got[changed], z["adaptive_val_b%d" % b])
+        d_raw = dev(torch, got)
+        d_rb = torch.empty(d["n_rebin"], dtype=torch.float32, device="cuda")
+        L.call("ctbb_rebin_device", C.byref(mr), ptr(d_raw), ptr(d_rb))
+        torch.cuda.synchronize()
+        vs = mr.cg.n_rows * mr.cg.n_channels_oversampled
+        assert_rebin_matches_golden(d_rb.cpu().numpy().reshape(-1, vs)[::step], z["rebin_b%d" % b])
+        L.call("ctbb_rebin_filter", C.byref(mr))
+        L.call("ctbb_backproject", C.byref(mr))
+    d = H.dims(mr)
+    assert_hu(H.view(mr.ctd.image, d["n_image"]), z["image"])
+    L.call("ctbb_finalize_image_stack", C.byref(mr))
+    assert_hu(H.view(mr.ctd.final_image_stack, z["final"].size), z["final"])
+    scan.close()
+
+
+def test_rebin_filter_testing_flag_copies_filtered_rows(torch_cuda, oracle_lib, lib, tmp_path):
+    """flags.testing: the drop-in rebin_filter also fills host ctd.rebin (the
+    reference's rebin.ct_test checkpoint)."""
+    scan = H.Scan(scans.tiny(0, 1, seed=51), str(tmp_path))
+    mr = scan.mr
+    raw = scan.next_block()
+    st = H.oracle_block(oracle_lib, scan, raw, adaptive=False)
+    mr.flags.testing = 1
+    L.call("ctbb_rebin_filter", C.byref(mr))
+    assert_filter_close(H.view(mr.ctd.rebin, H.dims(mr)["n_rebin"]).copy(), st["filtered"])
+    L.call("ctbb_backproject", C.byref(mr))
+    assert not mr.ctd.d_rebin
+    scan.close()
+
+
+def test_backproject_without_rebin_is_a_state_error(torch_cuda, lib, tmp_path):
+    scan = H.Scan(scans.tiny(0, 0, seed=52), str(tmp_path))
+    scan.next_block()
+    st = L.load().ctbb_backproject(C.byref(scan.mr))
+    assert L.STATUS[st] == "CTBB_ERR_STATE"
+    scan.close()
+
+
+def test_config1_geometry_reduced_image(torch_cuda, oracle_lib, lib, tmp_path):
+    """Config-1 scanner and helix (672 ch x 16 rows, 1152 views/turn, pitch 1,
+    3 turns, pull window past the end of the data) on a 48^2 image."""
+    spec = scans.ScanSpec(**{**scans.CONFIGS["config1"].__dict__})
+    spec.nx = spec.ny = 48
+    spec.recon_fov = 48 * 0.68 * 4
+    spec.n_slices = 4
+    scan = H.Scan(spec, str(tmp_path))
+    mr = scan.mr
+    raw = scan.next_block()
+    assert mr.ri.idx_pull_start + mr.ri.n_proj_pull > spec.n_readings  # frames past the end read 0
+    st = H.oracle_block(oracle_lib, scan, raw)
+    scan.set_raw(raw)
+    L.call("ctbb_adaptive_filter_kk", C.byref(mr))
+    np.testing.assert_array_equal(H.view(mr.ctd.raw, H.dims(mr)["n_raw"]), st["adaptive"])
+    L.call("ctbb_rebin_filter", C.byref(mr))
+    L.call("ctbb_backproject", C.byref(mr))
+    d = H.dims(mr)
+    assert_hu(H.view(mr.ctd.image, d["n_block"]), st["block"])
+    scan.close()
