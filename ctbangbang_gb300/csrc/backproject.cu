@@ -45,7 +45,9 @@ struct BpParams {
     int nx, ny, n_slices, nos, n_rows, nht, n_half;
     float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
     float ds_half;         // r_f fai / 2
+    float inv_ds_half;     // 1 / ds_half
     float two_cc;          // 2 * central channel
+    float coll;            // slice spacing
     float rf, inv_rf, rf2; // r_f, 1 / r_f, r_f^2
     float z_rot, two_pi;   // z_rot, 2 pi'
     float zrot_over_2pi;
@@ -78,8 +80,15 @@ __device__ __forceinline__ bool last_turn_sample_valid(const BpParams &p, float 
 
 constexpr float kBorderBand = 1e-3f;
 
+// p_idx = p / (r_f fai / 2) + 2 cc as the reference rounds it (division, then
+// add), used where the interp2 border decision is close.
+__device__ __forceinline__ float p_index_exact(const BpParams &p, float phat)
+{
+    return __fadd_rn(__fdiv_rn(phat, p.ds_half), p.two_cc);
+}
+
 template <int ZPT>
-__global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
+__global__ void __launch_bounds__(256, 2) backproject_kernel(BpParams p)
 {
     int xi = blockIdx.x * blockDim.x + threadIdx.x;
     int yi = blockIdx.y * blockDim.y + threadIdx.y;
@@ -89,12 +98,12 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
     float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
     float y = __fadd_rn(__fmul_rn(p.pix_y, __fsub_rn((float)yi, p.y_c)), p.y0);
 
-    float zp[ZPT], img[ZPT];
+    float img[ZPT];
 #pragma unroll
-    for (int z = 0; z < ZPT; ++z) {
-        zp[z] = (z0 + z < p.n_slices) ? __ldg(p.zpos + z0 + z) : 0.0f;
-        img[z] = 0.0f;
-    }
+    for (int z = 0; z < ZPT; ++z) img[z] = 0.0f;
+    // slice z of the column sits at zbase + z * coll (the exact per-slice value
+    // is only needed by the border recheck and is read from zpos there)
+    const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
     const size_t view_stride = (size_t)p.n_rows * p.nos;
     const float p_max = (float)(p.nos - 2);
     const float q_max_last = (float)(p.n_rows - 2);
@@ -108,22 +117,30 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
         }
         for (int k = 0; k < p.nht; ++k) {
             float4 t = __ldg(p.views + (size_t)i * p.nht + k);
-            // p and its detector index exactly as the reference rounds them: the
-            // p border of interp2 is then decided identically
+            // p exactly as the reference rounds it; p_idx from a reciprocal,
+            // re-evaluated exactly when it is within kBorderBand of a border
             float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
-            float p_idx = __fadd_rn(__fdiv_rn(phat, p.ds_half), p.two_cc);
+            float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
+            if (fabsf(p_idx) < kBorderBand || fabsf(p_idx - p_max) < kBorderBand) p_idx = p_index_exact(p, phat);
             bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
             float ray = (t.x - asinf(phat * p.inv_rf)) * p.zrot_over_2pi;
             float lhat = sqrtf(p.rf2 - phat * phat) - x * t.z - y * t.y;
-            float inv_den = 1.0f / (lhat * p.tan_cone);
-            float q_off = -ray * inv_den;
+            float inv_den = __frcp_rn(lhat * p.tan_cone);
+            // local row coordinate ql = (q + 1) (R - 1) / 2 of slice z is linear in z
+            float q0 = (zbase - ray) * inv_den;
+            float dq = p.coll * inv_den;
             bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
             const float *view = p.rebin + ((size_t)i + (size_t)k * p.n_half) * view_stride + ip;
+            // p-interpolated values of the current row pair (rows cur, cur + 1):
+            // slices advance about one detector row each, so each new slice
+            // usually loads only the row it enters
+            int cur = -2;
+            float c0 = 0.0f, c1 = 0.0f;
 #pragma unroll
             for (int z = 0; z < ZPT; ++z) {
-                float q = fmaf(zp[z], inv_den, q_off);
+                float q = fmaf((float)z, dq, q0);
                 float aq = fabsf(q);
                 if (aq < 1.0f) {
                     float w = 1.0f;
@@ -132,24 +149,32 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
                         w = c * c;
                     }
                     h[z] += w;
-                    float ql = (q + 1.0f) * p.half_rows;
+                    float ql = fmaf(q, p.half_rows, p.half_rows);
                     bool ok = p_ok;
                     if (ok && last) {
-                        float dq = ql - q_max_last;
-                        if (dq > kBorderBand) ok = false;
-                        else if (dq > -kBorderBand)
-                            ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, zp[z], k);
+                        float d = ql - q_max_last;
+                        if (d > kBorderBand) ok = false;
+                        else if (d > -kBorderBand)
+                            ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + z), k);
                     }
                     if (ok) {
                         // (q + 1) (R - 1) / 2 can round up to R - 1 for q just below 1:
                         // keep the second row inside the view
                         int iq = min((int)ql, p.n_rows - 2);
                         float wq = ql - (float)iq;
-                        const float *r0 = view + (size_t)iq * p.nos;
-                        float v00 = __ldg(r0), v01 = __ldg(r0 + 1);
-                        float v10 = __ldg(r0 + p.nos), v11 = __ldg(r0 + p.nos + 1);
-                        float c0 = fmaf(wp, v01 - v00, v00);
-                        float c1 = fmaf(wp, v11 - v10, v10);
+                        if (iq != cur) {
+                            const float *r1 = view + (size_t)(iq + 1) * p.nos;
+                            if (iq == cur + 1) {
+                                c0 = c1;
+                            } else {
+                                const float *r0 = r1 - p.nos;
+                                float v00 = __ldg(r0), v01 = __ldg(r0 + 1);
+                                c0 = fmaf(wp, v01 - v00, v00);
+                            }
+                            float v10 = __ldg(r1), v11 = __ldg(r1 + 1);
+                            c1 = fmaf(wp, v11 - v10, v10);
+                            cur = iq;
+                        }
                         s[z] = fmaf(w, fmaf(wq, c1 - c0, c0), s[z]);
                     }
                 }
@@ -157,7 +182,7 @@ __global__ void __launch_bounds__(256) backproject_kernel(BpParams p)
         }
 #pragma unroll
         for (int z = 0; z < ZPT; ++z)
-            if (h[z] != 0.0f) img[z] += s[z] / h[z];
+            if (h[z] != 0.0f) img[z] += __fdividef(s[z], h[z]);
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
@@ -225,6 +250,8 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     p.x0 = rp.x_origin;
     p.y0 = rp.y_origin;
     p.ds_half = cg.r_f * cg.fan_angle_increment / 2.0f;
+    p.inv_ds_half = 1.0f / p.ds_half;
+    p.coll = rp.coll_slicewidth;
     p.two_cc = 2.0f * cg.central_channel;
     p.rf = cg.r_f;
     p.inv_rf = 1.0f / cg.r_f;

@@ -11,9 +11,11 @@
 // are packed into one complex row (x_a + i x_b); because the kernel is real the
 // real and imaginary parts of the inverse transform are the two filtered rows.
 // Each CTA is persistent, loads the twiddle table once and then loops over row
-// pairs: load (coalesced) -> forward Stockham passes (radix 4, one radix-2 pass
-// when log2 M is odd) -> multiply by the kernel spectrum H/M (fused into the
-// first inverse pass) -> inverse passes -> store.  HBM traffic is one read and
+// pairs: load (coalesced) -> forward Stockham passes (radix 16 in registers, one
+// radix-2/4/8 pass first when log2 M is not a multiple of 4; three passes for
+// M = 4096) -> multiply by the kernel spectrum H/M (fused into the first
+// inverse pass) -> inverse passes -> store.  Shared-memory indices are padded
+// by one element per 32 so the strided Stockham stores are conflict-free.  HBM traffic is one read and
 // one write of the rows; the transform lives in shared memory.
 #include <cuda_runtime.h>
 
@@ -78,8 +80,54 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// One Stockham pass of radix R over m points, src -> dst.  sign = -1 forward,
-// +1 inverse.  tw[t] = exp(-2 pi i t / m); the inverse uses the conjugate.
+// Shared-memory index with one float2 of padding per 32: Stockham stores of
+// radix 16 go to stride-16 addresses, which would otherwise all hit one bank.
+__device__ __forceinline__ int pad(int e) { return e + (e >> 5); }
+
+// R-point DFT in registers, V[m] = sum_r v[r] exp(sign 2 pi i r m / R), R a
+// power of two <= 16: radix-2 decimation in time over bit-reversed inputs with
+// compile-time twiddles.
+template <int R>
+__device__ __forceinline__ void dft_registers(float2 (&v)[R], int sign)
+{
+    // bit-reversal permutation
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        int j = 0;
+#pragma unroll
+        for (int b = 1, t = i; b < R; b <<= 1, t >>= 1) j = (j << 1) | (t & 1);
+        if (j > i) {
+            float2 tmp = v[i];
+            v[i] = v[j];
+            v[j] = tmp;
+        }
+    }
+    // exp(-2 pi i k / 16), k = 0..7
+    const float c16[8] = {1.0f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508977f,
+                          0.0f, -0.38268343236508977f, -0.70710678118654752f, -0.92387953251128674f};
+    const float s16[8] = {0.0f, -0.38268343236508977f, -0.70710678118654752f, -0.92387953251128674f,
+                          -1.0f, -0.92387953251128674f, -0.70710678118654752f, -0.38268343236508977f};
+#pragma unroll
+    for (int half = 1; half < R; half <<= 1) {
+#pragma unroll
+        for (int k = 0; k < half; ++k) {
+            int idx = k * (16 / (2 * half));  // exponent in units of 2 pi / 16
+            float wr = c16[idx], wi = sign < 0 ? s16[idx] : -s16[idx];
+#pragma unroll
+            for (int j = k; j < R; j += 2 * half) {
+                float2 a = v[j];
+                float2 b = v[j + half];
+                if (idx != 0) b = make_float2(b.x * wr - b.y * wi, b.x * wi + b.y * wr);
+                v[j] = make_float2(a.x + b.x, a.y + b.y);
+                v[j + half] = make_float2(a.x - b.x, a.y - b.y);
+            }
+        }
+    }
+}
+
+// One Stockham pass of radix R over m points, src -> dst (padded indices).
+// tw[t] = exp(-2 pi i t / m); the inverse uses the conjugate.  pre_mul (the
+// kernel spectrum) multiplies the inputs of the first inverse pass.
 template <int R>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                               const float2 *__restrict__ tw, int m, int ns, int sign,
@@ -92,56 +140,46 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            v[r] = src[j + r * nb];
+            v[r] = src[pad(j + r * nb)];
             if (pre_mul) v[r] = cmul(v[r], __ldg(pre_mul + j + r * nb));
         }
+        if (k != 0) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) {
-            float2 w = tw[(r * k * tstride) & (m - 1)];
-            if (sign > 0) w.y = -w.y;
-            v[r] = cmul(v[r], w);
+            for (int r = 1; r < R; ++r) {
+                float2 w = tw[r * k * tstride];
+                if (sign > 0) w.y = -w.y;
+                v[r] = cmul(v[r], w);
+            }
         }
-        if (R == 2) {
-            float2 a = v[0], b = v[1];
-            v[0] = make_float2(a.x + b.x, a.y + b.y);
-            v[1] = make_float2(a.x - b.x, a.y - b.y);
-        } else {
-            float2 a = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-            float2 b = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-            float2 c = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-            float2 e = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
-            // d = e * (sign * i)
-            float2 d = sign < 0 ? make_float2(e.y, -e.x) : make_float2(-e.y, e.x);
-            v[0] = make_float2(a.x + c.x, a.y + c.y);
-            v[2] = make_float2(a.x - c.x, a.y - c.y);
-            v[1] = make_float2(b.x + d.x, b.y + d.y);
-            v[3] = make_float2(b.x - d.x, b.y - d.y);
-        }
+        dft_registers<R>(v, sign);
         int base = (j / ns) * ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[base + r * ns] = v[r];
+        for (int r = 0; r < R; ++r) dst[pad(base + r * ns)] = v[r];
     }
 }
 
-// Full transform; returns the buffer holding the result.
+// Full transform (radix 16 passes, one radix 2/4/8 pass first when log2 m is
+// not a multiple of 4); returns the buffer holding the result.
 __device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int log2m, int sign,
                             const float2 *pre_mul)
 {
     int ns = 1;
-    bool first = true;
-    if (log2m & 1) {
-        stockham_pass<2>(a, b, tw, m, ns, sign, pre_mul);
+    int rem = log2m & 3;
+    if (rem) {
+        if (rem == 1) stockham_pass<2>(a, b, tw, m, ns, sign, pre_mul);
+        else if (rem == 2) stockham_pass<4>(a, b, tw, m, ns, sign, pre_mul);
+        else stockham_pass<8>(a, b, tw, m, ns, sign, pre_mul);
         __syncthreads();
         float2 *t = a; a = b; b = t;
-        ns *= 2;
-        first = false;
+        ns <<= rem;
+        pre_mul = nullptr;
     }
     while (ns < m) {
-        stockham_pass<4>(a, b, tw, m, ns, sign, first ? pre_mul : nullptr);
+        stockham_pass<16>(a, b, tw, m, ns, sign, pre_mul);
         __syncthreads();
         float2 *t = a; a = b; b = t;
-        ns *= 4;
-        first = false;
+        ns *= 16;
+        pre_mul = nullptr;
     }
     return a;
 }
@@ -149,9 +187,10 @@ __device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int l
 __global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, const float2 *__restrict__ g_tw)
 {
     extern __shared__ float2 smem[];
+    const int padded = pad(p.m - 1) + 1;
     float2 *tw = smem;
     float2 *buf_a = smem + p.m;
-    float2 *buf_b = smem + 2 * p.m;
+    float2 *buf_b = buf_a + padded;
     for (int i = threadIdx.x; i < p.m; i += blockDim.x) tw[i] = g_tw[i];
     size_t n_pairs = (p.n_lines + 1) / 2;
     for (size_t pair = blockIdx.x; pair < n_pairs; pair += gridDim.x) {
@@ -166,7 +205,7 @@ __global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, cons
                 xa = ra[i];
                 if (has_b) xb = rb[i];
             }
-            buf_a[i] = make_float2(xa, xb);
+            buf_a[pad(i)] = make_float2(xa, xb);
         }
         __syncthreads();
         float2 *res = fft_smem(buf_a, buf_b, tw, p.m, p.log2m, -1, nullptr);
@@ -175,7 +214,7 @@ __global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, cons
         float *wa = p.lines + la * (size_t)p.n;
         float *wb = p.lines + lb * (size_t)p.n;
         for (int i = threadIdx.x; i < p.n; i += blockDim.x) {
-            float2 v = res[i];
+            float2 v = res[pad(i)];
             wa[i] = v.x;
             if (has_b) wb[i] = v.y;
         }
@@ -244,11 +283,13 @@ int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_line
     p.log2m = 0;
     while ((1 << p.log2m) < p.m) p.log2m++;
     p.spectrum = plan.d_spectrum;
-    size_t smem = sizeof(float2) * 3 * (size_t)p.m;
+    auto padded = [](size_t m) { return m + ((m - 1) >> 5) + 1; };
+    size_t smem = sizeof(float2) * ((size_t)p.m + 2 * padded((size_t)p.m));
     static bool attr_set = false;
     if (!attr_set) {
+        size_t max_smem = sizeof(float2) * (kMaxRampTransform + 2 * padded(kMaxRampTransform));
         CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(sizeof(float2) * 3 * kMaxRampTransform)));
+                                           (int)max_smem));
         attr_set = true;
     }
     int per_sm = (int)std::max<size_t>(1, (size_t)(200 * 1024) / smem);

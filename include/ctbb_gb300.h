@@ -38,9 +38,10 @@
 /* Boundary types (layout of the reference's parse_config.h / recon_structs.h) */
 /* ------------------------------------------------------------------------- */
 
-#ifndef CTBB_REFERENCE_STRUCTS_DEFINED
-#define CTBB_REFERENCE_STRUCTS_DEFINED
-
+/* A driver that already included the reference's parse_config.h /
+   recon_structs.h (include guards parse_config_h / recon_structs_h) keeps its
+   own identical definitions. */
+#if !defined(parse_config_h)
 /* .prm keys, parse_config.h:36-67 of the reference. */
 struct recon_params {
     char raw_data_dir[4096];
@@ -73,7 +74,9 @@ struct recon_params {
     char table_dir_str[1024];   /* TableDir: "in" / "out"                      */
     int table_dir;              /* TableDirInt: -1 in, 1 out                   */
 };
+#endif /* parse_config_h */
 
+#if !defined(recon_structs_h)
 struct block_info {
     int block_idx;
     float block_slice_start;
@@ -159,7 +162,7 @@ struct recon_metadata {
     double *table_positions;
 };
 
-#endif /* CTBB_REFERENCE_STRUCTS_DEFINED */
+#endif /* recon_structs_h */
 
 /* ------------------------------------------------------------------------- */
 /* Status codes                                                              */

@@ -5,6 +5,7 @@ import ctypes as C
 import glob
 import json
 import os
+import platform
 
 import numpy as np
 import pytest
@@ -17,12 +18,23 @@ from tests.conftest import REPO
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
 
+# The golden fixtures were made on x86_64.  The rebin tables (fan angles and
+# their inverse search) come from the host libm's asinf/sinf/cosf, which on
+# aarch64 may differ from x86_64 glibc by an ulp; on another architecture the
+# unfiltered rebin is therefore compared to 2e-6 relative instead of exactly.
+# (On any one machine the GPU rebin is bit-exact with the oracle.)
+SAME_LIBM_AS_GOLDEN = platform.machine() in ("x86_64", "AMD64")
+
+
 def assert_rebin_matches_golden(got, golden):
     """Unfiltered rebin vs the golden made through a unit-impulse kernel: that
     pass is exact except on samples that were exactly 0 (frames past the end
     of the data), where the reference's double FFT leaves ~1e-16 of roundoff."""
     zero = np.abs(golden) < 1e-9
-    np.testing.assert_array_equal(got[~zero], golden[~zero])
+    if SAME_LIBM_AS_GOLDEN:
+        np.testing.assert_array_equal(got[~zero], golden[~zero])
+    else:
+        np.testing.assert_allclose(got[~zero], golden[~zero], rtol=2e-6, atol=1e-7)
     assert np.all(np.abs(got[zero]) < 1e-9)
 
 
@@ -73,12 +85,25 @@ def test_oracle_matches_reference_golden(lib, oracle_lib, tmp_path, path):
         np.testing.assert_array_equal(st["adaptive"][changed], z["adaptive_val_b%d" % b])
         vs = mr.cg.n_rows * mr.cg.n_channels_oversampled
         assert_rebin_matches_golden(st["rebin"].reshape(-1, vs)[::step], z["rebin_b%d" % b])
-        np.testing.assert_array_equal(st["filtered"].reshape(-1, vs)[::step], z["filtered_b%d" % b])
-    np.testing.assert_array_equal(H.view(mr.ctd.image, d["n_image"]), z["image"])
+        got_f = st["filtered"].reshape(-1, vs)[::step]
+        if SAME_LIBM_AS_GOLDEN:
+            np.testing.assert_array_equal(got_f, z["filtered_b%d" % b])
+        else:
+            np.testing.assert_allclose(got_f, z["filtered_b%d" % b], rtol=0, atol=2e-6 * np.abs(got_f).max())
+    if SAME_LIBM_AS_GOLDEN:
+        np.testing.assert_array_equal(H.view(mr.ctd.image, d["n_image"]), z["image"])
+    else:
+        mx, rms = H.hu_errors(H.view(mr.ctd.image, d["n_image"]), z["image"])
+        assert mx <= 1.0 and rms <= 0.1
     oracle_lib.oracle_finalize(C.byref(mr))
     n_final = L.load().ctbb_n_slices_final(C.byref(mr))
     assert n_final == meta["n_final"]
-    np.testing.assert_array_equal(H.view(mr.ctd.final_image_stack, n_final * d["plane"]), z["final"])
+    fin = H.view(mr.ctd.final_image_stack, n_final * d["plane"])
+    if SAME_LIBM_AS_GOLDEN:
+        np.testing.assert_array_equal(fin, z["final"])
+    else:
+        mx, rms = H.hu_errors(fin, z["final"])
+        assert mx <= 1.0 and rms <= 0.1
     scan.close()
 
 
