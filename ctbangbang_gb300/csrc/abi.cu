@@ -82,8 +82,10 @@ struct Context {
 
 Context &ctx()
 {
-    static Context *c = new Context;  // never destroyed: no CUDA calls at exit
-    return *c;
+    // static storage, constructed on first use without heap allocation; its
+    // destructor makes no CUDA calls (device buffers are released explicitly)
+    static Context c;
+    return c;
 }
 
 cudaEvent_t pooled_event(Context &c)

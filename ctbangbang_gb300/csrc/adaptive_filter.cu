@@ -157,8 +157,6 @@ __global__ void af_threshold_kernel(AfParams p)
 constexpr int TP = 4, TR = 8, TC = 32;
 constexpr int SP = TP + 4, SR = TR + 4, SC = TC + 4;
 
-__constant__ float c_tri[125];  // weight of tap (ii, jj, kk) at [ii][jj][kk]
-
 __global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
 {
     __shared__ float tile[SP][SR][SC];
@@ -189,12 +187,17 @@ __global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
                 if (gp + d - 2 >= 0 && gp + d - 2 < p.P) { nk++; sk += tri1(d); }
             }
             float norm = (float)(nj * nk * si + ni * nk * sj + ni * nj * sk + ni * nj * nk);
+            // taps in the reference's order (channel, row, frame); the weights
+            // are compile-time constants of the fully unrolled loops
             float val = 0.0f;
+#pragma unroll
             for (int ii = 0; ii < 5; ii++)
+#pragma unroll
                 for (int jj = 0; jj < 5; jj++)
 #pragma unroll
                     for (int kk = 0; kk < 5; kk++)
-                        val = __fadd_rn(val, __fmul_rn(tile[lp + kk][lr + jj][lc + ii], c_tri[ii * 25 + jj * 5 + kk]));
+                        val = __fadd_rn(val, __fmul_rn(tile[lp + kk][lr + jj][lc + ii],
+                                                       (float)(tri1(ii) + tri1(jj) + tri1(kk) + 1)));
             y = __fmul_rn(__fdiv_rn(1.0f, norm), val);
         }
         p.out[(size_t)gp * frame + (size_t)gr * p.N + gc] = y;
@@ -208,16 +211,6 @@ size_t adaptive_filter_scratch_floats(size_t n_proj_pull) { return 6 * n_proj_pu
 int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
                            float *d_scratch, cudaStream_t stream)
 {
-    static bool tri_uploaded = false;
-    if (!tri_uploaded) {
-        float tri[125];
-        for (int ii = 0; ii < 5; ii++)
-            for (int jj = 0; jj < 5; jj++)
-                for (int kk = 0; kk < 5; kk++)
-                    tri[ii * 25 + jj * 5 + kk] = (float)(tri1(ii) + tri1(jj) + tri1(kk) + 1);
-        CTBB_CUDA_TRY(cudaMemcpyToSymbol(c_tri, tri, sizeof(tri)));
-        tri_uploaded = true;
-    }
     AfParams p;
     p.raw = d_in;
     p.out = d_out;
@@ -261,3 +254,4 @@ int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, f
 }
 
 }  // namespace ctbb
+
