@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "adaptive_filter.h"
 #include "ctbb_internal.h"
@@ -255,3 +256,82 @@ int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, f
 
 }  // namespace ctbb
 
+// --------------------------------------------------------------------------
+// Adaptive filter without any allocation
+// --------------------------------------------------------------------------
+//
+// For callers that must not allocate device memory while a scan is being
+// processed -- a scanner-side service that reserves all device memory at
+// start-up and keeps cudaMalloc (which can synchronise the whole device and
+// has unbounded latency) out of its per-scan path, or a host process whose
+// device memory belongs to another allocator (a framework's caching pool, a
+// fixed MPS/MIG quota) -- this variant takes its per-frame statistics from a
+// fixed array in the library's static device memory instead of the library's
+// allocated workspace.  The caller still passes the input and output buffers.
+
+namespace ctbb {
+
+// Largest pull window (frames) the static scratch holds; config-3 blocks pull
+// 8448 frames and config-2 blocks 11264.
+constexpr size_t kNoAllocMaxFrames = 65536;
+
+// 6 statistics per frame (sup, smooth, ecc, max, min, threshold): 1.5 MiB.
+// Every GPU that loads the library holds this array until the process exits.
+static __device__ __align__(256) float g_af_noalloc_scratch[6 * kNoAllocMaxFrames];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the static scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+int noalloc_scratch(float **out)
+{
+    int dev = 0;
+    CTBB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("adaptive filter (no allocation): device %d beyond %d", dev, kMaxDevices);
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        CTBB_CUDA_TRY(cudaGetSymbolAddress(&p, g_af_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<float *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return CTBB_OK;
+}
+
+}  // namespace
+}  // namespace ctbb
+
+extern "C" int ctbb_adaptive_filter_device_noalloc(const struct recon_metadata *mr, const float *d_in,
+                                                   float *d_out)
+{
+    using namespace ctbb;
+    clear_error();
+    if (!mr || !d_in || !d_out) {
+        set_error("ctbb_adaptive_filter_device_noalloc: null argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    if (mr->ri.n_proj_pull == 0 || mr->cg.n_channels == 0 || mr->cg.n_rows_raw == 0) {
+        set_error("ctbb_adaptive_filter_device_noalloc: recon_metadata is not planned");
+        return CTBB_ERR_STATE;
+    }
+    if (mr->ri.n_proj_pull > kNoAllocMaxFrames) {
+        set_error("ctbb_adaptive_filter_device_noalloc: pull window of %zu frames exceeds the "
+                  "fixed scratch of %zu frames; use ctbb_adaptive_filter_device",
+                  mr->ri.n_proj_pull, kNoAllocMaxFrames);
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(require_device());
+    float *scratch = nullptr;
+    CTBB_TRY(noalloc_scratch(&scratch));
+    // Every statistic is written for all frames before it is read, so the
+    // previous call's contents need no clearing.
+    return launch_adaptive_filter(*mr, d_in, d_out, scratch, current_stream());
+}

@@ -42,6 +42,7 @@ PROTOTYPES = {
     "ctbb_finalize_image_stack": (C.c_int, [_MR]),
     "ctbb_finalize_image_stack_hu": (C.c_int, [_MR, C.c_float]),
     "ctbb_adaptive_filter_device": (C.c_int, [_MR, _VP, _VP]),
+    "ctbb_adaptive_filter_device_noalloc": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_rebin_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_ramp_filter_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),

@@ -295,6 +295,23 @@ int ctbb_finalize_image_stack_hu(struct recon_metadata *mr, float mu_water);
 int ctbb_adaptive_filter_device(const struct recon_metadata *mr,
                                 const float *d_raw_in, float *d_raw_out);
 
+/* Adaptive filter of one pull window that allocates nothing.  No counterpart
+   in the reference.  For callers that cannot allocate device memory while a
+   scan is processed (a service that reserves all device memory at start-up
+   and keeps cudaMalloc -- which can synchronise the device -- out of its
+   per-scan path, or a process whose device memory belongs to another
+   allocator): the per-frame statistics live in a fixed static device array of
+   the library (6 floats per frame for at most 65536 frames, 1.5 MiB, held by
+   every GPU that loads the library until the process exits) instead of the
+   library's allocated workspace.  The caller passes d_raw_in and d_raw_out.
+   Windows longer than 65536 frames are rejected with CTBB_ERR_ARGUMENT.  The
+   first call on a device looks up the array's device address
+   (cudaGetSymbolAddress), so make that first call before any stream capture.
+   All calls share the array: calls that overlap on the GPU race.  Output is
+   identical to ctbb_adaptive_filter_device. */
+int ctbb_adaptive_filter_device_noalloc(const struct recon_metadata *mr,
+                                        const float *d_raw_in, float *d_raw_out);
+
 /* Rebin (no filter) of one pull window into d_rebin [n_views][n_rows][n_os]. */
 int ctbb_rebin_device(const struct recon_metadata *mr, const float *d_raw,
                       float *d_rebin);
