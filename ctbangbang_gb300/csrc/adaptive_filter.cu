@@ -21,7 +21,8 @@
 // without fused multiply-adds.  GB300 mapping: step 1 is a CTA reduction per
 // frame, steps 2-3 one thread per frame, step 4 one warp per frame (the window
 // counts are integers, so splitting them across lanes is exact), step 5 a
-// shared-memory tiled stencil.
+// per-frame float4 stream that smooths only the samples above the threshold
+// (rows of a multiple of 4 channels; otherwise a shared-memory tiled stencil).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -59,7 +60,15 @@ __global__ void af_sup_kernel(AfParams p)
     size_t frame = (size_t)p.R * p.N;
     const float *src = p.raw + (size_t)proj * frame;
     float m = 0.0f;
-    for (size_t i = threadIdx.x; i < frame; i += blockDim.x) m = fmaxf(m, src[i]);
+    if ((frame & 3) == 0) {  // frames start 16-byte aligned: float4 loads
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        for (size_t i = threadIdx.x; i < frame / 4; i += blockDim.x) {
+            float4 v = __ldg(s4 + i);
+            m = fmaxf(fmaxf(m, fmaxf(v.x, v.y)), fmaxf(v.z, v.w));
+        }
+    } else {
+        for (size_t i = threadIdx.x; i < frame; i += blockDim.x) m = fmaxf(m, src[i]);
+    }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ float red[32];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -205,6 +214,66 @@ __global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
     }
 }
 
+// 5x5x5 triangle smoothing of one sample, taps in the reference's order
+// (channel, row, frame) with out-of-range taps skipped; norm is the exact
+// integer sum of the in-range weights.
+__device__ __noinline__ float smooth_sample(const AfParams &p, int gp, int gr, int gc)
+{
+    size_t frame = (size_t)p.R * p.N;
+    int ni = 0, nj = 0, nk = 0, si = 0, sj = 0, sk = 0;
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        if (gc + d - 2 >= 0 && gc + d - 2 < p.N) { ni++; si += tri1(d); }
+        if (gr + d - 2 >= 0 && gr + d - 2 < p.R) { nj++; sj += tri1(d); }
+        if (gp + d - 2 >= 0 && gp + d - 2 < p.P) { nk++; sk += tri1(d); }
+    }
+    float norm = (float)(nj * nk * si + ni * nk * sj + ni * nj * sk + ni * nj * nk);
+    float val = 0.0f;
+#pragma unroll 1
+    for (int ii = 0; ii < 5; ii++) {
+        int c = gc + ii - 2;
+#pragma unroll 1
+        for (int jj = 0; jj < 5; jj++) {
+            int r = gr + jj - 2;
+#pragma unroll
+            for (int kk = 0; kk < 5; kk++) {
+                int f = gp + kk - 2;
+                if (c < 0 || c >= p.N || r < 0 || r >= p.R || f < 0 || f >= p.P) continue;
+                float x = __ldg(p.raw + (size_t)f * frame + (size_t)r * p.N + c);
+                val = __fadd_rn(val, __fmul_rn(x, (float)(tri1(ii) + tri1(jj) + tri1(kk) + 1)));
+            }
+        }
+    }
+    return __fmul_rn(__fdiv_rn(1.0f, norm), val);
+}
+
+// Streaming form for rows of a multiple of 4 channels: one CTA per frame
+// copies the frame with float4 loads/stores and smooths only the samples above
+// the frame's threshold -- about 1e-4 of them on clinical-size scans -- so the
+// kernel runs at copy speed.  Same arithmetic, same result as the tiled form.
+__global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
+{
+    int gp = blockIdx.x;
+    size_t frame = (size_t)p.R * p.N;
+    const float4 *src = reinterpret_cast<const float4 *>(p.raw + (size_t)gp * frame);
+    float4 *dst = reinterpret_cast<float4 *>(p.out + (size_t)gp * frame);
+    const float T = __ldg(p.thr + gp);
+    const int n4 = (int)(frame / 4);
+    const int row4 = p.N / 4;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+        float4 v = __ldg(src + i);
+        if (v.x > T || v.y > T || v.z > T || v.w > T) {
+            int gr = i / row4;
+            int gc = (i - gr * row4) * 4;
+            if (v.x > T) v.x = smooth_sample(p, gp, gr, gc);
+            if (v.y > T) v.y = smooth_sample(p, gp, gr, gc + 1);
+            if (v.z > T) v.z = smooth_sample(p, gp, gr, gc + 2);
+            if (v.w > T) v.w = smooth_sample(p, gp, gr, gc + 3);
+        }
+        dst[i] = v;
+    }
+}
+
 }  // namespace
 
 size_t adaptive_filter_scratch_floats(size_t n_proj_pull) { return 6 * n_proj_pull; }
@@ -243,12 +312,16 @@ int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, f
     af_smooth_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
     af_ecc_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
     af_threshold_kernel<<<(p.P * 32 + 255) / 256, 256, 0, stream>>>(p);
-    dim3 grid((p.N + TC - 1) / TC, (p.R + TR - 1) / TR, (p.P + TP - 1) / TP);
-    if (grid.z > 65535) {
-        set_error("adaptive filter: %d frames exceed the launch grid", p.P);
-        return CTBB_ERR_ARGUMENT;
+    if (p.N % 4 == 0) {
+        af_filter_stream_kernel<<<p.P, 256, 0, stream>>>(p);
+    } else {
+        dim3 grid((p.N + TC - 1) / TC, (p.R + TR - 1) / TR, (p.P + TP - 1) / TP);
+        if (grid.z > 65535) {
+            set_error("adaptive filter: %d frames exceed the launch grid", p.P);
+            return CTBB_ERR_ARGUMENT;
+        }
+        af_filter_kernel<<<grid, 256, 0, stream>>>(p);
     }
-    af_filter_kernel<<<grid, 256, 0, stream>>>(p);
     count_launch(5);
     CTBB_CUDA_TRY(cudaGetLastError());
     return CTBB_OK;

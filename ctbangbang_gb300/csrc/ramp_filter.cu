@@ -80,9 +80,11 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// Shared-memory index with one float2 of padding per 32: Stockham stores of
-// radix 16 go to stride-16 addresses, which would otherwise all hit one bank.
-__device__ __forceinline__ int pad(int e) { return e + (e >> 5); }
+// Shared-memory index with one float2 of padding per 16.  64-bit accesses are
+// served per half-warp; with this padding the 16 lanes of every load and
+// store of every Stockham pass (radix 2..16, any power-of-two size up to the
+// maximum) fall on 16 distinct bank pairs.
+__device__ __forceinline__ int pad(int e) { return e + (e >> 4); }
 
 // R-point DFT in registers, V[m] = sum_r v[r] exp(sign 2 pi i r m / R), R a
 // power of two <= 16: radix-2 decimation in time over bit-reversed inputs with
@@ -144,12 +146,25 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
             if (pre_mul) v[r] = cmul(v[r], __ldg(pre_mul + j + r * nb));
         }
         if (k != 0) {
+            // twiddles w^r, w = exp(sign 2 pi i k tstride / m): w, w^2, w^4, w^8 are
+            // read from the table, the others formed by at most two products
+            float2 wp[R];
+            wp[0] = make_float2(1.0f, 0.0f);
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = tw[r * k * tstride];
+            for (int b = 1; b < R; b <<= 1) {
+                float2 w = __ldg(tw + b * k * tstride);
                 if (sign > 0) w.y = -w.y;
-                v[r] = cmul(v[r], w);
+                wp[b] = w;
             }
+#pragma unroll
+            for (int r = 3; r < R; ++r) {
+                if ((r & (r - 1)) == 0) continue;
+                int hi = 1;
+                while ((hi << 1) <= r) hi <<= 1;
+                wp[r] = cmul(wp[hi], wp[r - hi]);
+            }
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], wp[r]);
         }
         dft_registers<R>(v, sign);
         int base = (j / ns) * ns * R + k;
@@ -184,14 +199,14 @@ __device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int l
     return a;
 }
 
-__global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, const float2 *__restrict__ g_tw)
+__global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, const float2 *__restrict__ tw)
 {
+    // twiddles come from the read-only cache (one table for every CTA), which
+    // leaves shared memory to the two transform buffers
     extern __shared__ float2 smem[];
     const int padded = pad(p.m - 1) + 1;
-    float2 *tw = smem;
-    float2 *buf_a = smem + p.m;
+    float2 *buf_a = smem;
     float2 *buf_b = buf_a + padded;
-    for (int i = threadIdx.x; i < p.m; i += blockDim.x) tw[i] = g_tw[i];
     size_t n_pairs = (p.n_lines + 1) / 2;
     for (size_t pair = blockIdx.x; pair < n_pairs; pair += gridDim.x) {
         size_t la = 2 * pair, lb = la + 1;
@@ -283,16 +298,16 @@ int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_line
     p.log2m = 0;
     while ((1 << p.log2m) < p.m) p.log2m++;
     p.spectrum = plan.d_spectrum;
-    auto padded = [](size_t m) { return m + ((m - 1) >> 5) + 1; };
-    size_t smem = sizeof(float2) * ((size_t)p.m + 2 * padded((size_t)p.m));
+    auto padded = [](size_t m) { return m + ((m - 1) >> 4) + 1; };
+    size_t smem = sizeof(float2) * 2 * padded((size_t)p.m);
     static bool attr_set = false;
     if (!attr_set) {
-        size_t max_smem = sizeof(float2) * (kMaxRampTransform + 2 * padded(kMaxRampTransform));
+        size_t max_smem = sizeof(float2) * 2 * padded(kMaxRampTransform);
         CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)max_smem));
         attr_set = true;
     }
-    int per_sm = (int)std::max<size_t>(1, (size_t)(200 * 1024) / smem);
+    int per_sm = (int)std::max<size_t>(1, (size_t)(220 * 1024) / smem);
     if (per_sm > 4) per_sm = 4;
     size_t n_pairs = (n_lines + 1) / 2;
     int grid = (int)std::min<size_t>(n_pairs, (size_t)num_sms() * per_sm);

@@ -248,55 +248,52 @@ __device__ __forceinline__ void view_taps(float a, int n, int *i0, int *i1, floa
     *i1 = (a == (float)n - 1.0f) ? *i0 : *i0 + 1;
 }
 
-// Linear interpolation along the view axis of focal spot q at fixed (row, ch):
-// interp3 with integer channel and row reduces to a1*(1-w) + a5*w.
-__device__ __forceinline__ float lerp_views(const RebinParams &p, int q, int row, int ch, float alpha)
-{
-    int i0, i1;
-    float w;
-    view_taps(alpha, p.n_proj, &i0, &i1, &w);
-    size_t frame_stride = (size_t)p.R_raw * p.N;
-    size_t off = (size_t)row * p.N + ch;
-    float a1 = __ldg(p.raw + ((size_t)p.n_ffs * i0 + q) * frame_stride + off);
-    float a5 = __ldg(p.raw + ((size_t)p.n_ffs * i1 + q) * frame_stride + off);
-    return __fadd_rn(__fmul_rn(a1, __fsub_rn(1.0f, w)), __fmul_rn(a5, w));
-}
+// Views per thread: the per-channel taps and focal terms are loaded once and
+// reused along the view axis.
+constexpr int kViewsPerThread = 8;
 
 // --------------------------------------------------------------------------
-// Kernels
+// Kernels.  Idx is the index type of the raw and output arrays (32-bit when
+// both hold fewer than 2^31 samples).
 // --------------------------------------------------------------------------
 
 // no-FFS and z-FFS: bilinear in (channel, view).  grid: x channel blocks,
-// y raw row, z view; each thread writes one sample for each focal spot.
+// y raw row, z chunks of kViewsPerThread views.
+template <class Idx>
 __global__ void rebin_bilinear_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int row = blockIdx.y;
-    int v = blockIdx.z;
+    int v0 = blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
-    int proj = v + p.add;
-    size_t frame_stride = (size_t)p.R_raw * p.N;
+    const Idx frame_stride = (Idx)p.R_raw * p.N;
+    const Idx nos = (Idx)p.Nos;
     for (int s = 0; s < p.n_ffs; ++s) {
-        const AxisTap tap = p.taps[(size_t)s * p.Nos + c];
-        const FocalTerm ft = p.focal[(size_t)s * p.Nos + c];
-        float alpha = focal_alpha(p.n_ffs, proj, ft.t_alpha, p.n_ffs == 1 ? 0.0f : p.focal_offset[s], s);
-        int i0, i1;
-        float w;
-        view_taps(alpha, p.n_proj, &i0, &i1, &w);
-        size_t off = (size_t)row * p.N;
-        const float *f0 = p.raw + ((size_t)p.n_ffs * i0 + s) * frame_stride + off;
-        const float *f1 = p.raw + ((size_t)p.n_ffs * i1 + s) * frame_stride + off;
-        float a1 = __ldg(f0 + tap.i0), a2 = __ldg(f0 + tap.i1);
-        float a5 = __ldg(f1 + tap.i0), a6 = __ldg(f1 + tap.i1);
-        float omw = __fsub_rn(1.0f, w);
-        float t1 = __fmul_rn(__fmul_rn(a1, tap.one_minus_u), omw);
-        float t2 = __fmul_rn(__fmul_rn(a2, tap.u), omw);
-        float t5 = __fmul_rn(__fmul_rn(a5, tap.one_minus_u), w);
-        float t6 = __fmul_rn(__fmul_rn(a6, tap.u), w);
-        float val = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t5), t6);
+        const AxisTap tap = p.taps[s * p.Nos + c];
+        const float t_alpha = p.focal[s * p.Nos + c].t_alpha;
+        const float t_off = p.n_ffs == 1 ? 0.0f : p.focal_offset[s];
+        const float omu = tap.one_minus_u, u = tap.u;
         int out_row = row;
         if (p.n_ffs == 2) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
-        p.out[((size_t)v * p.R + out_row) * p.Nos + c] = val;
+        const float *base = p.raw + (Idx)row * p.N + s * frame_stride;
+        float *out = p.out + (Idx)out_row * nos + c;
+#pragma unroll 4
+        for (int v = v0; v < min(v0 + kViewsPerThread, p.n_views); ++v) {
+            float alpha = focal_alpha(p.n_ffs, v + p.add, t_alpha, t_off, s);
+            int i0, i1;
+            float w;
+            view_taps(alpha, p.n_proj, &i0, &i1, &w);
+            const float *f0 = base + (Idx)(p.n_ffs * i0) * frame_stride;
+            const float *f1 = base + (Idx)(p.n_ffs * i1) * frame_stride;
+            float a1 = __ldg(f0 + tap.i0), a2 = __ldg(f0 + tap.i1);
+            float a5 = __ldg(f1 + tap.i0), a6 = __ldg(f1 + tap.i1);
+            float omw = __fsub_rn(1.0f, w);
+            float t1 = __fmul_rn(__fmul_rn(a1, omu), omw);
+            float t2 = __fmul_rn(__fmul_rn(a2, u), omw);
+            float t5 = __fmul_rn(__fmul_rn(a5, omu), w);
+            float t6 = __fmul_rn(__fmul_rn(a6, u), w);
+            out[(Idx)v * p.R * nos] = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t5), t6);
+        }
     }
 }
 
@@ -304,28 +301,41 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
 // (virtual) azimuthally rebinned intermediate, each a view-axis lerp of one
 // focal spot.  For phi+z-FFS side s = 0 (-dr) uses focal spots 0/1 and s = 1
 // (+dr) focal spots 2/3.
+template <class Idx>
 __global__ void rebin_two_stage_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int row = blockIdx.y;
-    int v = blockIdx.z;
+    int v0 = blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
-    int proj = v + p.add;
+    const Idx frame_stride = (Idx)p.R_raw * p.N;
+    const Idx nos = (Idx)p.Nos;
     int sides = p.n_ffs == 4 ? 2 : 1;
     for (int s = 0; s < sides; ++s) {
-        const AxisTap tap = p.taps[(size_t)s * p.Nos + c];
+        const AxisTap tap = p.taps[s * p.Nos + c];
         int qb = 2 * s;
-        int j0 = tap.i0, j1 = tap.i1;
-        int q0 = qb + (j0 & 1), ch0 = j0 >> 1;
-        int q1 = qb + (j1 & 1), ch1 = j1 >> 1;
-        float a0 = focal_alpha(p.n_ffs, proj, p.focal[(size_t)q0 * p.N + ch0].t_alpha, p.focal_offset[q0], q0);
-        float a1 = focal_alpha(p.n_ffs, proj, p.focal[(size_t)q1 * p.N + ch1].t_alpha, p.focal_offset[q1], q1);
-        float T0 = lerp_views(p, q0, row, ch0, a0);
-        float T1 = lerp_views(p, q1, row, ch1, a1);
-        float val = __fadd_rn(__fmul_rn(T0, tap.one_minus_u), __fmul_rn(T1, tap.u));
+        int q0 = qb + (tap.i0 & 1), ch0 = tap.i0 >> 1;
+        int q1 = qb + (tap.i1 & 1), ch1 = tap.i1 >> 1;
+        const float ta0 = p.focal[q0 * p.N + ch0].t_alpha, to0 = p.focal_offset[q0];
+        const float ta1 = p.focal[q1 * p.N + ch1].t_alpha, to1 = p.focal_offset[q1];
+        const float *b0 = p.raw + (Idx)row * p.N + ch0 + q0 * frame_stride;
+        const float *b1 = p.raw + (Idx)row * p.N + ch1 + q1 * frame_stride;
         int out_row = row;
         if (p.n_ffs == 4) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
-        p.out[((size_t)v * p.R + out_row) * p.Nos + c] = val;
+        float *out = p.out + (Idx)out_row * nos + c;
+#pragma unroll 4
+        for (int v = v0; v < min(v0 + kViewsPerThread, p.n_views); ++v) {
+            int proj = v + p.add;
+            int i0, i1;
+            float w0, w1;
+            view_taps(focal_alpha(p.n_ffs, proj, ta0, to0, q0), p.n_proj, &i0, &i1, &w0);
+            float T0 = __fadd_rn(__fmul_rn(__ldg(b0 + (Idx)(p.n_ffs * i0) * frame_stride), __fsub_rn(1.0f, w0)),
+                                 __fmul_rn(__ldg(b0 + (Idx)(p.n_ffs * i1) * frame_stride), w0));
+            view_taps(focal_alpha(p.n_ffs, proj, ta1, to1, q1), p.n_proj, &i0, &i1, &w1);
+            float T1 = __fadd_rn(__fmul_rn(__ldg(b1 + (Idx)(p.n_ffs * i0) * frame_stride), __fsub_rn(1.0f, w1)),
+                                 __fmul_rn(__ldg(b1 + (Idx)(p.n_ffs * i1) * frame_stride), w1));
+            out[(Idx)v * p.R * nos] = __fadd_rn(__fmul_rn(T0, tap.one_minus_u), __fmul_rn(T1, tap.u));
+        }
     }
 }
 
@@ -347,16 +357,21 @@ int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float 
     p.add = t.add_projections;
     p.n_views = t.n_views;
     p.reverse_rows = t.reverse_rows;
-    if (t.n_views > 65535 || t.n_rows_raw > 65535) {
+    int chunks = (t.n_views + kViewsPerThread - 1) / kViewsPerThread;
+    if (chunks > 65535 || t.n_rows_raw > 65535) {
         set_error("rebin: %d views / %d rows exceed the launch grid", t.n_views, t.n_rows_raw);
         return CTBB_ERR_ARGUMENT;
     }
+    size_t n_raw = (size_t)t.n_ffs * t.n_proj * t.n_rows_raw * t.n_channels;
+    size_t n_out = (size_t)t.n_views * t.n_rows * t.n_os;
+    bool narrow = n_raw < ((size_t)1 << 31) && n_out < ((size_t)1 << 31);
     dim3 block(128);
-    dim3 grid((t.n_os + 127) / 128, t.n_rows_raw, t.n_views);
-    if (t.mode == RebinMode::kNoFfs || t.mode == RebinMode::kZFfs)
-        rebin_bilinear_kernel<<<grid, block, 0, stream>>>(p);
-    else
-        rebin_two_stage_kernel<<<grid, block, 0, stream>>>(p);
+    dim3 grid((t.n_os + 127) / 128, t.n_rows_raw, chunks);
+    bool bilinear = t.mode == RebinMode::kNoFfs || t.mode == RebinMode::kZFfs;
+    if (bilinear && narrow) rebin_bilinear_kernel<int><<<grid, block, 0, stream>>>(p);
+    else if (bilinear) rebin_bilinear_kernel<size_t><<<grid, block, 0, stream>>>(p);
+    else if (narrow) rebin_two_stage_kernel<int><<<grid, block, 0, stream>>>(p);
+    else rebin_two_stage_kernel<size_t><<<grid, block, 0, stream>>>(p);
     count_launch();
     CTBB_CUDA_TRY(cudaGetLastError());
     return CTBB_OK;
