@@ -27,6 +27,10 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "backproject.h"
@@ -55,6 +59,7 @@ struct BpParams {
     float half_rows;       // (R - 1) / 2
     float taper_scale;     // (pi'/2) / (1 - Q)
     float out_scale;       // 2 pi' / n_proj_turn
+    int flat_path;         // R >= 8: rows of |q| <= Q never reach a border
 };
 
 constexpr float kQ = 0.6f;
@@ -79,6 +84,10 @@ __device__ __forceinline__ bool last_turn_sample_valid(const BpParams &p, float 
 }
 
 constexpr float kBorderBand = 1e-3f;
+// inner chunks: |q| <= kInnerMax keeps every row below R-1 after rounding;
+// rows kRowMargin below the last-turn border are far from its band
+constexpr float kInnerMax = 0.999f;
+constexpr float kRowMargin = 0.01f;
 
 // p_idx = p / (r_f fai / 2) + 2 cc as the reference rounds it (division, then
 // add), used where the interp2 border decision is close.
@@ -101,8 +110,20 @@ __device__ __forceinline__ float asin_fast(float a)
     return fmaf(a * t, p, a);
 }
 
-template <int ZPT>
-__global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(BpParams p)
+// The 2x2 footprint {(p, row), (p+1, row), (p, row+1), (p+1, row+1)} of a
+// view, row in [0, R-2]; `view` points at (p, 0).
+__device__ __forceinline__ void fetch_footprint(const float *view, int nos, float row, float &v00, float &v01,
+                                                float &v10, float &v11)
+{
+    const float *r0 = view + (int)row * nos;
+    v00 = __ldg(r0);
+    v01 = __ldg(r0 + 1);
+    v10 = __ldg(r0 + nos);
+    v11 = __ldg(r0 + nos + 1);
+}
+
+template <int ZPT, int MIN_BLOCKS>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
     int xi = blockIdx.x * blockDim.x + threadIdx.x;
     int yi = blockIdx.y * blockDim.y + threadIdx.y;
@@ -112,9 +133,13 @@ __global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(Bp
     float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
     float y = __fadd_rn(__fmul_rn(p.pix_y, __fsub_rn((float)yi, p.y_c)), p.y0);
 
-    float img[ZPT];
+    // the image sums live in shared memory (touched once per angle), which
+    // leaves the registers to the per-angle sums and the gathers in flight
+    __shared__ float img_sh[ZPT][256];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    float *img = &img_sh[0][tid];
 #pragma unroll
-    for (int z = 0; z < ZPT; ++z) img[z] = 0.0f;
+    for (int z = 0; z < ZPT; ++z) img[z * 256] = 0.0f;
     // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
     // is only needed by the border recheck and is read from zpos there)
     const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
@@ -129,18 +154,30 @@ __global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(Bp
             s[z] = 0.0f;
             h[z] = 0.0f;
         }
+        // The views i + k n_half are half turns apart: p flips its sign from
+        // one to the next and |p| stays, so asin(|p| / r_f) and sqrt(r_f^2 - p^2)
+        // are taken once per angle (from k = 0) and given the sign of each p.
+        const float4 *vt = p.views + (size_t)i * p.nht;
+        float a_abs, root;
+        {
+            float4 t0 = __ldg(vt);
+            float phat0 = __fsub_rn(__fmul_rn(x, t0.y), __fmul_rn(y, t0.z));
+            a_abs = fabsf(asin_fast(phat0 * p.inv_rf));
+            float l2 = fmaf(-phat0, phat0, p.rf2);
+            root = l2 * rsqrtf(l2);
+        }
         for (int k = 0; k < p.nht; ++k) {
-            float4 t = __ldg(p.views + (size_t)i * p.nht + k);
+            float4 t = __ldg(vt + k);
             // q of the chunk's slices: q(z) = q0 + z dq (dq > 0)
             float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
-            float ray = (t.x - asin_fast(phat * p.inv_rf)) * p.zrot_over_2pi;
-            float l2 = fmaf(-phat, phat, p.rf2);
-            float lhat = l2 * rsqrtf(l2) - x * t.z - y * t.y;
+            float ray = (t.x - copysignf(a_abs, phat)) * p.zrot_over_2pi;
+            float lhat = root - x * t.z - y * t.y;
             float inv_den = __fdividef(1.0f, lhat * p.tan_cone);
             float q0 = (zbase - ray) * inv_den;
             float dq = p.coll * inv_den;
+            float q_end = fmaf((float)(ZPT - 1), dq, q0);
             // no slice of the chunk inside |q| < 1: nothing to add, not even weight
-            if (q0 >= 1.0f || fmaf((float)(ZPT - 1), dq, q0) <= -1.0f) continue;
+            if (q0 >= 1.0f || q_end <= -1.0f) continue;
             // p and its border decision exactly as the reference rounds them
             float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
             if (fabsf(p_idx) < kBorderBand || fabsf(p_idx - p_max) < kBorderBand) p_idx = p_index_exact(p, phat);
@@ -148,11 +185,67 @@ __global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(Bp
             bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
-            const float *view = p.rebin + ((size_t)i + (size_t)k * p.n_half) * view_stride + ip;
-            // Branch-free gathers: every slice loads its 2x2 footprint from an
-            // address that is always inside the view (row clamped to [0, R-2],
-            // channel 0 when p is off the detector) and validity only scales
-            // the weight, so the loads of all slices can be issued together.
+            const float *view = p.rebin + (size_t)(i + k * p.n_half) * view_stride + ip;
+            // Chunk classes, decided per warp so that no two paths both run
+            // (q is monotone in z, so |q| is largest at an end of the chunk):
+            //  flat:  every |q| <= Q, so W = 1; with R >= 8 every row lies in
+            //         [0, R-2] and below the last-turn border;
+            //  inner: every |q| < 1, so every row lies in [0, R-2]; in the last
+            //         half turn also every row well below its border;
+            //  other: per-slice validity, clamped rows, last-turn border.
+            float a_max = fmaxf(fabsf(q0), fabsf(q_end));
+            unsigned lanes = __activemask();
+            if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
+                if (p_ok) {
+#pragma unroll
+                    for (int z = 0; z < ZPT; ++z) {
+                        float q = fmaf((float)z, dq, q0);
+                        float ql = fmaf(q, p.half_rows, p.half_rows);
+                        float row = floorf(ql);
+                        float wq = ql - row;
+                        float v00, v01, v10, v11;
+                        fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                        float c0 = fmaf(wp, v01 - v00, v00);
+                        float c1 = fmaf(wp, v11 - v10, v10);
+                        s[z] += fmaf(wq, c1 - c0, c0);
+                    }
+                }
+#pragma unroll
+                for (int z = 0; z < ZPT; ++z) h[z] += 1.0f;
+                continue;
+            }
+            bool inner = a_max < kInnerMax && (!last || fmaf(a_max, p.half_rows, p.half_rows) < q_max_last - kRowMargin);
+            if (__all_sync(lanes, inner)) {
+                if (p_ok) {
+#pragma unroll
+                    for (int z = 0; z < ZPT; ++z) {
+                        float q = fmaf((float)z, dq, q0);
+                        float c = __cosf(fmaxf(fabsf(q) - kQ, 0.0f) * p.taper_scale);
+                        float w = c * c;
+                        h[z] += w;
+                        float ql = fmaf(q, p.half_rows, p.half_rows);
+                        float row = floorf(ql);
+                        float wq = ql - row;
+                        float v00, v01, v10, v11;
+                        fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                        float c0 = fmaf(wp, v01 - v00, v00);
+                        float c1 = fmaf(wp, v11 - v10, v10);
+                        s[z] = fmaf(w, fmaf(wq, c1 - c0, c0), s[z]);
+                    }
+                } else {
+#pragma unroll
+                    for (int z = 0; z < ZPT; ++z) {
+                        float q = fmaf((float)z, dq, q0);
+                        float c = __cosf(fmaxf(fabsf(q) - kQ, 0.0f) * p.taper_scale);
+                        h[z] += c * c;
+                    }
+                }
+                continue;
+            }
+            // Other chunks.  Branch-free gathers: every slice loads its 2x2
+            // footprint from inside the view (row clamped to [0, R-2], channel 0
+            // when p is off the detector) and validity only scales the weight, so
+            // the loads of all slices can be issued together.
 #pragma unroll
             for (int z = 0; z < ZPT; ++z) {
                 float q = fmaf((float)z, dq, q0);
@@ -163,11 +256,10 @@ __global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(Bp
                 float w = in ? c * c : 0.0f;
                 h[z] += w;
                 float ql = fmaf(q, p.half_rows, p.half_rows);
-                int iq = min(max((int)ql, 0), p.n_rows - 2);
-                float wq = ql - (float)iq;
-                const float *r0 = view + iq * p.nos;
-                float v00 = __ldg(r0), v01 = __ldg(r0 + 1);
-                float v10 = __ldg(r0 + p.nos), v11 = __ldg(r0 + p.nos + 1);
+                float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
+                float wq = ql - row;
+                float v00, v01, v10, v11;
+                fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
                 bool ok = p_ok && in;
                 if (last && ok) {
                     float d = ql - q_max_last;
@@ -182,12 +274,21 @@ __global__ void __launch_bounds__(256, (ZPT <= 8 ? 3 : 2)) backproject_kernel(Bp
         }
 #pragma unroll
         for (int z = 0; z < ZPT; ++z)
-            if (h[z] != 0.0f) img[z] += __fdividef(s[z], h[z]);
+            if (h[z] != 0.0f) img[z * 256] += __fdividef(s[z], h[z]);
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
     for (int z = 0; z < ZPT; ++z)
-        if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z] * p.out_scale;
+        if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z * 256] * p.out_scale;
+}
+
+int bp_min_blocks()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_MINB");
+        return e ? atoi(e) : 3;
+    }();
+    return v;
 }
 
 }  // namespace
@@ -261,6 +362,10 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     p.zrot_over_2pi = cg.z_rot / (2.0f * pi);
     p.tan_cone = std::tan(cg.theta_cone / 2.0f);
     p.half_rows = ((float)cg.n_rows - 1.0f) / 2.0f;
+    // |q| <= Q maps to rows within (R-1)(1 +- Q)/2; for R >= 8 that is inside
+    // [0, R-2] with a margin of more than a tenth of a row, including the
+    // last-turn border at R-2
+    p.flat_path = cg.n_rows >= 8 ? 1 : 0;
     p.taper_scale = (pi / 2.0f) / (1.0f - kQ);
     p.out_scale = 2.0f * pi / (float)cg.n_proj_turn;
     if (p.n_rows < 2 || p.nos < 2) {
@@ -269,23 +374,17 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     }
     dim3 block(32, 8);
     dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8, 1);
+    auto go = [&](auto zpt_tag) {
+        constexpr int Z = decltype(zpt_tag)::value;
+        grid.z = (p.n_slices + Z - 1) / Z;
+        constexpr int MB = Z <= 8 ? 3 : 2;
+        if (Z == 8 && bp_min_blocks() == 4) backproject_kernel<8, 4><<<grid, block, 0, stream>>>(p);
+        else backproject_kernel<Z, MB><<<grid, block, 0, stream>>>(p);
+    };
     switch (zpt) {
-    case 32:
-        grid.z = (p.n_slices + 31) / 32;
-        backproject_kernel<32><<<grid, block, 0, stream>>>(p);
-        break;
-    case 16:
-        grid.z = (p.n_slices + 15) / 16;
-        backproject_kernel<16><<<grid, block, 0, stream>>>(p);
-        break;
-    case 4:
-        grid.z = (p.n_slices + 3) / 4;
-        backproject_kernel<4><<<grid, block, 0, stream>>>(p);
-        break;
-    default:
-        grid.z = (p.n_slices + 7) / 8;
-        backproject_kernel<8><<<grid, block, 0, stream>>>(p);
-        break;
+    case 16: go(std::integral_constant<int, 16>()); break;
+    case 4: go(std::integral_constant<int, 4>()); break;
+    default: go(std::integral_constant<int, 8>()); break;
     }
     count_launch();
     CTBB_CUDA_TRY(cudaGetLastError());

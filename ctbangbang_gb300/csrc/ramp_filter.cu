@@ -131,14 +131,28 @@ __device__ __forceinline__ void dft_registers(float2 (&v)[R], int sign)
 // tw[t] = exp(-2 pi i t / m); the inverse uses the conjugate.  pre_mul (the
 // kernel spectrum) multiplies the inputs of the first inverse pass.
 template <int R>
+struct Log2;
+template <> struct Log2<2> { static constexpr int v = 1; };
+template <> struct Log2<4> { static constexpr int v = 2; };
+template <> struct Log2<8> { static constexpr int v = 3; };
+template <> struct Log2<16> { static constexpr int v = 4; };
+
+// One Stockham pass of radix R over m = 2^log2m points, src -> dst (padded
+// indices); ns = 2^log2ns is the size of the sub-transforms already done.
+// All index arithmetic is shifts and masks.  tw[t] = exp(-2 pi i t / m); the
+// inverse uses the conjugate.  pre_mul (the kernel spectrum) multiplies the
+// inputs of the first inverse pass.
+template <int R>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
-                                              const float2 *__restrict__ tw, int m, int ns, int sign,
+                                              const float2 *__restrict__ tw, int log2m, int log2ns, int sign,
                                               const float2 *__restrict__ pre_mul)
 {
-    const int nb = m / R;
-    const int tstride = m / (ns * R);
+    constexpr int lr = Log2<R>::v;
+    const int nb = 1 << (log2m - lr);
+    const int log2t = log2m - log2ns - lr;  // twiddle stride m / (ns R)
+    const int ns_mask = (1 << log2ns) - 1;
     for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-        int k = j % ns;
+        int k = j & ns_mask;
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -152,7 +166,7 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
             wp[0] = make_float2(1.0f, 0.0f);
 #pragma unroll
             for (int b = 1; b < R; b <<= 1) {
-                float2 w = __ldg(tw + b * k * tstride);
+                float2 w = __ldg(tw + ((b * k) << log2t));
                 if (sign > 0) w.y = -w.y;
                 wp[b] = w;
             }
@@ -167,9 +181,9 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
             for (int r = 1; r < R; ++r) v[r] = cmul(v[r], wp[r]);
         }
         dft_registers<R>(v, sign);
-        int base = (j / ns) * ns * R + k;
+        int base = ((j >> log2ns) << (log2ns + lr)) + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[pad(base + r * ns)] = v[r];
+        for (int r = 0; r < R; ++r) dst[pad(base + (r << log2ns))] = v[r];
     }
 }
 
@@ -178,28 +192,29 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
 __device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int log2m, int sign,
                             const float2 *pre_mul)
 {
-    int ns = 1;
+    int log2ns = 0;
     int rem = log2m & 3;
     if (rem) {
-        if (rem == 1) stockham_pass<2>(a, b, tw, m, ns, sign, pre_mul);
-        else if (rem == 2) stockham_pass<4>(a, b, tw, m, ns, sign, pre_mul);
-        else stockham_pass<8>(a, b, tw, m, ns, sign, pre_mul);
+        if (rem == 1) stockham_pass<2>(a, b, tw, log2m, log2ns, sign, pre_mul);
+        else if (rem == 2) stockham_pass<4>(a, b, tw, log2m, log2ns, sign, pre_mul);
+        else stockham_pass<8>(a, b, tw, log2m, log2ns, sign, pre_mul);
         __syncthreads();
         float2 *t = a; a = b; b = t;
-        ns <<= rem;
+        log2ns += rem;
         pre_mul = nullptr;
     }
-    while (ns < m) {
-        stockham_pass<16>(a, b, tw, m, ns, sign, pre_mul);
+    while (log2ns < log2m) {
+        stockham_pass<16>(a, b, tw, log2m, log2ns, sign, pre_mul);
         __syncthreads();
         float2 *t = a; a = b; b = t;
-        ns *= 16;
+        log2ns += 4;
         pre_mul = nullptr;
     }
+    (void)m;
     return a;
 }
 
-__global__ void __launch_bounds__(kFftThreads) ramp_fft_kernel(FftParams p, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(kFftThreads, 3) ramp_fft_kernel(FftParams p, const float2 *__restrict__ tw)
 {
     // twiddles come from the read-only cache (one table for every CTA), which
     // leaves shared memory to the two transform buffers
