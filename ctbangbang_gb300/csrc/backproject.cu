@@ -56,6 +56,9 @@ struct BpParams {
     float z_rot, two_pi;   // z_rot, 2 pi'
     float zrot_over_2pi;
     float tan_cone;
+    int k_window;          // half-turn window per angle (z_rot != 0)
+    float abs_zr;          // |z_rot / (2 pi')|
+    float inv_half_feed;   // 2 / z_rot: half turns per mm of ray travel
     float half_rows;       // (R - 1) / 2
     float taper_scale;     // (pi'/2) / (1 - Q)
     float out_scale;       // 2 pi' / n_proj_turn
@@ -88,6 +91,8 @@ constexpr float kBorderBand = 1e-3f;
 // rows kRowMargin below the last-turn border are far from its band
 constexpr float kInnerMax = 0.999f;
 constexpr float kRowMargin = 0.01f;
+// half-turn window margin (angle rounding is ~1e-6 half turns)
+constexpr float kWindowMargin = 0.01f;
 
 // p_idx = p / (r_f fai / 2) + 2 cc as the reference rounds it (division, then
 // add), used where the interp2 border decision is close.
@@ -146,6 +151,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
     const size_t view_stride = (size_t)p.n_rows * p.nos;
     const float p_max = (float)(p.nos - 2);
     const float q_max_last = (float)(p.n_rows - 2);
+    const float z_end = fmaf((float)(ZPT - 1), p.coll, zbase);
+    const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
+    const unsigned warp_lanes = __activemask();
 
     for (int i = 0; i < p.n_half; ++i) {
         float s[ZPT], h[ZPT];
@@ -159,14 +167,31 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
         // are taken once per angle (from k = 0) and given the sign of each p.
         const float4 *vt = p.views + (size_t)i * p.nht;
         float a_abs, root;
+        int k_lo = 0, k_hi = p.nht - 1;
         {
             float4 t0 = __ldg(vt);
             float phat0 = __fsub_rn(__fmul_rn(x, t0.y), __fmul_rn(y, t0.z));
             a_abs = fabsf(asin_fast(phat0 * p.inv_rf));
             float l2 = fmaf(-phat0, phat0, p.rf2);
             root = l2 * rsqrtf(l2);
+            if (p.k_window) {
+                // Half turns whose rays can reach the chunk: ray_k lies within
+                // |asin zr| of (theta_0 + k pi') zr, and |q| < 1 needs
+                // |z - ray_k| < lhat_k tan_cone <= (root + |x cos + y sin|) tan_cone.
+                // A margin of kWindowMargin half turns absorbs the rounding of the
+                // angles and of this bound; the exact test below still decides
+                // every visited half turn.
+                float reach = fmaf(root + fabsf(fmaf(x, t0.z, y * t0.y)), p.tan_cone, a_abs * p.abs_zr);
+                float base = t0.x * p.zrot_over_2pi;
+                float lo = (z_lo - reach - base) * p.inv_half_feed;
+                float hi = (z_hi + reach - base) * p.inv_half_feed;
+                k_lo = max(k_lo, (int)ceilf(fminf(lo, hi) - kWindowMargin));
+                k_hi = min(k_hi, (int)floorf(fmaxf(lo, hi) + kWindowMargin));
+            }
         }
-        for (int k = 0; k < p.nht; ++k) {
+        k_lo = __reduce_min_sync(warp_lanes, k_lo);
+        k_hi = __reduce_max_sync(warp_lanes, k_hi);
+        for (int k = k_lo; k <= k_hi; ++k) {
             float4 t = __ldg(vt + k);
             // q of the chunk's slices: q(z) = q0 + z dq (dq > 0)
             float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
@@ -245,7 +270,36 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             // Other chunks.  Branch-free gathers: every slice loads its 2x2
             // footprint from inside the view (row clamped to [0, R-2], channel 0
             // when p is off the detector) and validity only scales the weight, so
-            // the loads of all slices can be issued together.
+            // the loads of all slices can be issued together.  Only a warp with
+            // a row near the last-turn border takes the per-slice border test.
+            bool border = last && fmaf(q_end, p.half_rows, p.half_rows) > q_max_last - kBorderBand;
+            if (__any_sync(lanes, border)) {
+#pragma unroll
+                for (int z = 0; z < ZPT; ++z) {
+                    float q = fmaf((float)z, dq, q0);
+                    float aq = fabsf(q);
+                    bool in = aq < 1.0f;
+                    float c = __cosf(fmaxf(aq - kQ, 0.0f) * p.taper_scale);
+                    float w = in ? c * c : 0.0f;
+                    h[z] += w;
+                    float ql = fmaf(q, p.half_rows, p.half_rows);
+                    float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
+                    float wq = ql - row;
+                    float v00, v01, v10, v11;
+                    fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                    bool ok = p_ok && in;
+                    if (last && ok) {
+                        float d = ql - q_max_last;
+                        if (d > kBorderBand) ok = false;
+                        else if (d > -kBorderBand)
+                            ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + z), k);
+                    }
+                    float c0 = fmaf(wp, v01 - v00, v00);
+                    float c1 = fmaf(wp, v11 - v10, v10);
+                    s[z] = fmaf(ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
+                }
+                continue;
+            }
 #pragma unroll
             for (int z = 0; z < ZPT; ++z) {
                 float q = fmaf((float)z, dq, q0);
@@ -260,21 +314,16 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                 float wq = ql - row;
                 float v00, v01, v10, v11;
                 fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
-                bool ok = p_ok && in;
-                if (last && ok) {
-                    float d = ql - q_max_last;
-                    if (d > kBorderBand) ok = false;
-                    else if (d > -kBorderBand)
-                        ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + z), k);
-                }
                 float c0 = fmaf(wp, v01 - v00, v00);
                 float c1 = fmaf(wp, v11 - v10, v10);
-                s[z] = fmaf(ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
+                s[z] = fmaf(p_ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
             }
         }
 #pragma unroll
-        for (int z = 0; z < ZPT; ++z)
-            if (h[z] != 0.0f) img[z * 256] += __fdividef(s[z], h[z]);
+        for (int z = 0; z < ZPT; ++z) {
+            float r = __fdividef(s[z], h[z]);
+            img[z * 256] += h[z] != 0.0f ? r : 0.0f;
+        }
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
@@ -366,6 +415,9 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     // [0, R-2] with a margin of more than a tenth of a row, including the
     // last-turn border at R-2
     p.flat_path = cg.n_rows >= 8 ? 1 : 0;
+    p.k_window = std::fabs(cg.z_rot) > 1e-3f ? 1 : 0;
+    p.abs_zr = std::fabs(p.zrot_over_2pi);
+    p.inv_half_feed = p.k_window ? 2.0f / cg.z_rot : 0.0f;
     p.taper_scale = (pi / 2.0f) / (1.0f - kQ);
     p.out_scale = 2.0f * pi / (float)cg.n_proj_turn;
     if (p.n_rows < 2 || p.nos < 2) {
