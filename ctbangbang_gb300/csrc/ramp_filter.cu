@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -214,6 +215,198 @@ __device__ float2 *fft_smem(float2 *a, float2 *b, const float2 *tw, int m, int l
     return a;
 }
 
+// ---- 4096-point transforms (16 x 16 x 16): the size every row length in
+// 1025..2048 uses.  Thread j of 256 owns butterfly j of each pass; the three
+// forward passes read inputs j + 256 r (r = 0..15), so the last forward pass
+// leaves X[j + 256 r] in thread j's registers -- exactly the inputs of the first
+// inverse pass.  Spectrum multiply and that pass run in registers; the first
+// forward pass reads the rows from global memory (inputs r >= 8 are the zero
+// padding, since N <= M / 2) and the last inverse pass writes them back.
+constexpr int kM4096 = 4096;
+constexpr int kTw16Entries = 15 * 16 + 15 * 256;  // pass-2 and pass-3 twiddles
+
+// z * w for sign < 0, z * conj(w) for sign > 0
+template <int SIGN>
+__device__ __forceinline__ float2 twiddle(float2 z, float2 w)
+{
+    if (SIGN < 0) return make_float2(fmaf(z.x, w.x, -z.y * w.y), fmaf(z.x, w.y, z.y * w.x));
+    return make_float2(fmaf(z.x, w.x, z.y * w.y), fmaf(z.y, w.x, -z.x * w.y));
+}
+
+// omega4 * z with omega4 = exp(SIGN 2 pi i / 4) = SIGN i
+template <int SIGN>
+__device__ __forceinline__ float2 mul_omega4(float2 z)
+{
+    return SIGN < 0 ? make_float2(z.y, -z.x) : make_float2(-z.y, z.x);
+}
+
+// In-place 4-point DFT of (a, b, c, d), outputs in natural order.
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2 &a, float2 &b, float2 &c, float2 &d)
+{
+    float2 s0 = make_float2(a.x + c.x, a.y + c.y), d0 = make_float2(a.x - c.x, a.y - c.y);
+    float2 s1 = make_float2(b.x + d.x, b.y + d.y), d1 = mul_omega4<SIGN>(make_float2(b.x - d.x, b.y - d.y));
+    a = make_float2(s0.x + s1.x, s0.y + s1.y);
+    c = make_float2(s0.x - s1.x, s0.y - s1.y);
+    b = make_float2(d0.x + d1.x, d0.y + d1.y);
+    d = make_float2(d0.x - d1.x, d0.y - d1.y);
+}
+
+// z * exp(SIGN 2 pi i e / 16) for the internal twiddles of the 4 x 4 split
+template <int SIGN, int E>
+__device__ __forceinline__ float2 w16(float2 z)
+{
+    constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f, h = 0.70710678118654752f;
+    constexpr float sg = SIGN < 0 ? -1.0f : 1.0f;
+    if (E == 0) return z;
+    if (E == 4) return mul_omega4<SIGN>(z);
+    if (E == 2) return make_float2(h * (z.x - sg * z.y), h * (z.y + sg * z.x));
+    if (E == 6) return make_float2(-h * (z.x + sg * z.y), h * (sg * z.x - z.y));
+    // general: cos(2 pi E / 16), sin
+    constexpr float c = E == 1 ? c1 : E == 3 ? s1 : E == 9 ? -c1 : 0.0f;
+    constexpr float sn = sg * (E == 1 ? s1 : E == 3 ? c1 : E == 9 ? -s1 : 0.0f);
+    return make_float2(fmaf(z.x, c, -z.y * sn), fmaf(z.x, sn, z.y * c));
+}
+
+// 16-point DFT in registers, V[k] = sum_n v[n] exp(SIGN 2 pi i n k / 16), as
+// 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.  HALF: inputs 8..15 are zero.
+template <int SIGN, bool HALF>
+__device__ __forceinline__ void dft16(float2 (&v)[16])
+{
+    // DFT4 over n1 for each n2: elements n2, n2 + 4, n2 + 8, n2 + 12 -> k1
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+        if (HALF) {
+            float2 a = v[n2], b = v[n2 + 4];
+            float2 wb = mul_omega4<SIGN>(b);
+            v[n2] = make_float2(a.x + b.x, a.y + b.y);
+            v[n2 + 4] = make_float2(a.x + wb.x, a.y + wb.y);
+            v[n2 + 8] = make_float2(a.x - b.x, a.y - b.y);
+            v[n2 + 12] = make_float2(a.x - wb.x, a.y - wb.y);
+        } else {
+            dft4<SIGN>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+        }
+    }
+    // twiddles exp(SIGN 2 pi i n2 k1 / 16); element (n2, k1) sits at n2 + 4 k1
+    v[1 + 4 * 1] = w16<SIGN, 1>(v[1 + 4 * 1]);
+    v[1 + 4 * 2] = w16<SIGN, 2>(v[1 + 4 * 2]);
+    v[1 + 4 * 3] = w16<SIGN, 3>(v[1 + 4 * 3]);
+    v[2 + 4 * 1] = w16<SIGN, 2>(v[2 + 4 * 1]);
+    v[2 + 4 * 2] = w16<SIGN, 4>(v[2 + 4 * 2]);
+    v[2 + 4 * 3] = w16<SIGN, 6>(v[2 + 4 * 3]);
+    v[3 + 4 * 1] = w16<SIGN, 3>(v[3 + 4 * 1]);
+    v[3 + 4 * 2] = w16<SIGN, 6>(v[3 + 4 * 2]);
+    v[3 + 4 * 3] = w16<SIGN, 9>(v[3 + 4 * 3]);
+    // DFT4 over n2 for each k1: elements 4 k1 .. 4 k1 + 3 -> k2
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<SIGN>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // element (k1, k2) now sits at 4 k1 + k2; output k = k1 + 4 k2
+    float2 t[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) t[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = t[k];
+}
+
+// Twiddles of a pass: v[r] *= w^(r k) (conjugated for the inverse) from a
+// table laid out [r - 1][k] so that a warp reads consecutive k.
+template <int SIGN, int NK>
+__device__ __forceinline__ void apply_twiddles(float2 (&v)[16], const float2 *__restrict__ tab, int k)
+{
+#pragma unroll
+    for (int r = 1; r < 16; ++r) v[r] = twiddle<SIGN>(v[r], __ldg(tab + (r - 1) * NK + k));
+}
+
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(kFftThreads, MIN_BLOCKS)
+    ramp_fft4096_kernel(FftParams p, const float2 *__restrict__ tw2, const float2 *__restrict__ tw3)
+{
+    extern __shared__ float2 smem[];
+    float2 *buf_a = smem;
+    float2 *buf_b = smem + pad(kM4096 - 1) + 1;
+    const int j = threadIdx.x;
+    const int k2 = j & 15;                         // pass-2 sub-transform index
+    const int out2 = ((j >> 4) << 8) + k2;         // pass-2 output base
+    // padded shared-memory offsets as base + compile-time stride:
+    // pad(j + 256 r) = rd + 272 r, pad(16 j + r) = wr1 + r, pad(out2 + 16 r) = wr2 + 17 r
+    const int rd = j + (j >> 4);
+    const int wr1 = 17 * j;
+    const int wr2 = out2 + (out2 >> 4);
+    size_t n_pairs = (p.n_lines + 1) / 2;
+    for (size_t pair = blockIdx.x; pair < n_pairs; pair += gridDim.x) {
+        size_t la = 2 * pair, lb = la + 1;
+        bool has_b = lb < p.n_lines;
+        const float *ra = p.lines + la * (size_t)p.n;
+        const float *rb = p.lines + lb * (size_t)p.n;
+        float2 v[16];
+        // forward pass 1 (sub-transforms of size 1: no twiddles), from global
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            int idx = j + 256 * r;
+            float xa = 0.0f, xb = 0.0f;
+            if (idx < p.n) {
+                xa = __ldg(ra + idx);
+                if (has_b) xb = __ldg(rb + idx);
+            }
+            v[r] = make_float2(xa, xb);
+        }
+#pragma unroll
+        for (int r = 8; r < 16; ++r) v[r] = make_float2(0.0f, 0.0f);
+        dft16<-1, true>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) buf_a[wr1 + r] = v[r];
+        __syncthreads();
+        // forward pass 2 (size-16 sub-transforms)
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = buf_a[rd + 272 * r];
+        apply_twiddles<-1, 16>(v, tw2, k2);
+        dft16<-1, false>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) buf_b[wr2 + 17 * r] = v[r];
+        __syncthreads();
+        // forward pass 3 (size-256 sub-transforms): X[j + 256 r]
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = buf_b[rd + 272 * r];
+        apply_twiddles<-1, 256>(v, tw3, j);
+        dft16<-1, false>(v);
+        // kernel spectrum H / M, then inverse pass 1, all in registers
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = cmul(v[r], __ldg(p.spectrum + j + 256 * r));
+        dft16<1, false>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) buf_a[wr1 + r] = v[r];
+        __syncthreads();
+        // inverse pass 2
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = buf_a[rd + 272 * r];
+        apply_twiddles<1, 16>(v, tw2, k2);
+        dft16<1, false>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) buf_b[wr2 + 17 * r] = v[r];
+        __syncthreads();
+        // inverse pass 3: y[j + 256 r], only the first N are kept (r < 8)
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = buf_b[rd + 272 * r];
+        apply_twiddles<1, 256>(v, tw3, j);
+        dft16<1, false>(v);
+        float *wa = p.lines + la * (size_t)p.n;
+        float *wb = p.lines + lb * (size_t)p.n;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            int idx = j + 256 * r;
+            if (idx < p.n) {
+                wa[idx] = v[r].x;
+                if (has_b) wb[idx] = v[r].y;
+            }
+        }
+        // buf_a is rewritten next by pass 1 of the next pair: its last reads
+        // (inverse pass 2) precede the barrier after inverse pass 2; buf_b is
+        // rewritten after the barrier that follows that pass 1.
+    }
+}
+
 __global__ void __launch_bounds__(kFftThreads, 3) ramp_fft_kernel(FftParams p, const float2 *__restrict__ tw)
 {
     // twiddles come from the read-only cache (one table for every CTA), which
@@ -249,6 +442,16 @@ __global__ void __launch_bounds__(kFftThreads, 3) ramp_fft_kernel(FftParams p, c
             if (has_b) wb[i] = v.y;
         }
     }
+}
+
+// 4096-point kernel: 2 or 3 CTAs per SM (0: the generic kernel)
+int fft4096_mode()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_FFT4096");
+        return e ? atoi(e) : 2;
+    }();
+    return v;
 }
 
 }  // namespace
@@ -288,15 +491,32 @@ int prepare_ramp_filter(const float *h_taps, int n, RampFilterPlan *plan, cudaSt
         double a = -two_pi * (double)t / (double)m;
         tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
-    if (!plan->d_spectrum || plan->capacity < (size_t)m) {
+    // radix-16 tables of the 4096-point kernel, [r - 1][k]: pass 2
+    // exp(-2 pi i r k / 256) (k < 16), pass 3 exp(-2 pi i r k / 4096) (k < 256)
+    std::vector<float2> tw16(kTw16Entries);
+    for (int r = 1; r < 16; ++r) {
+        for (int k = 0; k < 16; ++k) {
+            double a = -two_pi * (double)(r * k) / 256.0;
+            tw16[(r - 1) * 16 + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        for (int k = 0; k < 256; ++k) {
+            double a = -two_pi * (double)(r * k) / 4096.0;
+            tw16[15 * 16 + (r - 1) * 256 + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+    }
+    size_t need = 2 * (size_t)m + kTw16Entries;
+    if (!plan->d_spectrum || plan->capacity < need) {
         if (plan->d_spectrum) cudaFree(plan->d_spectrum);
         plan->d_spectrum = nullptr;
-        CTBB_CUDA_TRY(cudaMalloc(&plan->d_spectrum, sizeof(float2) * 2 * (size_t)m));
-        plan->capacity = (size_t)m;
+        CTBB_CUDA_TRY(cudaMalloc(&plan->d_spectrum, sizeof(float2) * need));
+        plan->capacity = need;
     }
     plan->d_twiddle = plan->d_spectrum + m;
+    plan->d_tw16 = plan->d_twiddle + m;
     CTBB_CUDA_TRY(cudaMemcpyAsync(plan->d_spectrum, H.data(), sizeof(float2) * m, cudaMemcpyHostToDevice, stream));
     CTBB_CUDA_TRY(cudaMemcpyAsync(plan->d_twiddle, tw.data(), sizeof(float2) * m, cudaMemcpyHostToDevice, stream));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(plan->d_tw16, tw16.data(), sizeof(float2) * kTw16Entries,
+                                  cudaMemcpyHostToDevice, stream));
     // the host vectors die at return: make the copies complete first
     CTBB_CUDA_TRY(cudaStreamSynchronize(stream));
     return CTBB_OK;
@@ -320,13 +540,24 @@ int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_line
         size_t max_smem = sizeof(float2) * 2 * padded(kMaxRampTransform);
         CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)max_smem));
+        CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft4096_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(float2) * 2 * padded(kM4096))));
+        CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft4096_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(float2) * 2 * padded(kM4096))));
         attr_set = true;
     }
     int per_sm = (int)std::max<size_t>(1, (size_t)(220 * 1024) / smem);
     if (per_sm > 4) per_sm = 4;
     size_t n_pairs = (n_lines + 1) / 2;
     int grid = (int)std::min<size_t>(n_pairs, (size_t)num_sms() * per_sm);
-    ramp_fft_kernel<<<grid, kFftThreads, smem, stream>>>(p, plan.d_twiddle);
+    int mode = fft4096_mode();
+    if (p.m == kM4096 && mode == 3) {
+        ramp_fft4096_kernel<3><<<grid, kFftThreads, smem, stream>>>(p, plan.d_tw16, plan.d_tw16 + 15 * 16);
+    } else if (p.m == kM4096 && mode == 2) {
+        grid = (int)std::min<size_t>(n_pairs, (size_t)num_sms() * std::min(per_sm, 2));
+        ramp_fft4096_kernel<2><<<grid, kFftThreads, smem, stream>>>(p, plan.d_tw16, plan.d_tw16 + 15 * 16);
+    } else
+        ramp_fft_kernel<<<grid, kFftThreads, smem, stream>>>(p, plan.d_twiddle);
     count_launch();
     CTBB_CUDA_TRY(cudaGetLastError());
     return CTBB_OK;

@@ -16,7 +16,8 @@ struct RampFilterPlan {
     int m = 0;                     // transform size
     std::vector<float> taps;       // 2n host taps the spectrum was made from
     float2 *d_spectrum = nullptr;  // H/M [m], followed by the twiddle table [m]
-    float2 *d_twiddle = nullptr;
+    float2 *d_twiddle = nullptr;  // exp(-2 pi i t / m) [m]
+    float2 *d_tw16 = nullptr;     // radix-16 pass tables of the 4096-point kernel
     size_t capacity = 0;
 };
 

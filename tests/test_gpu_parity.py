@@ -300,3 +300,22 @@ def test_config2_geometry_backprojection(torch_cuda, oracle_lib, lib, tmp_path):
     assert np.abs(want).max() > 0.01  # the phantom is in the field
     assert_hu(got, want)
     scans.free_plan(mr)
+
+
+@pytest.mark.parametrize("n_os", [1025, 1472, 2048])
+def test_ramp_filter_4096_point_rows(torch_cuda, oracle_lib, n_os):
+    """Row lengths 1025..2048 take the 4096-point transform: the edge lengths
+    and the config-2 length, an odd number of rows (the last transform carries
+    one row), against the oracle's double-precision FFT convolution."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n_os)
+    n_lines = 301
+    rows = rng.standard_normal((n_lines, n_os)).astype(np.float32)
+    taps = np.zeros(2 * n_os, np.float32)
+    L.call("ctbb_ramp_filter_taps", n_os, C.c_float(0.3), C.c_float(1.0), C.c_float(1.0), fptr(taps))
+    d = dev(torch, rows.ravel())
+    L.call("ctbb_ramp_filter_device", ptr(d), n_lines, n_os, fptr(taps))
+    torch.cuda.synchronize()
+    want = rows.copy()
+    oracle_lib.oracle_filter_rows(fptr(want), n_lines, n_os, fptr(taps))
+    assert_filter_close(d.cpu().numpy().reshape(n_lines, n_os), want)
