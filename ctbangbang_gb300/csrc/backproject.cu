@@ -127,9 +127,12 @@ __device__ __forceinline__ void fetch_footprint(const float *view, int nos, floa
     v11 = __ldg(r0 + nos + 1);
 }
 
-template <int ZPT, int MIN_BLOCKS>
+// NOS > 0: the row length as a compile-time constant (the second row of a
+// footprint is then an immediate offset); 0: taken from p.nos.
+template <int ZPT, int MIN_BLOCKS, int NOS>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
+    const int nos = NOS > 0 ? NOS : p.nos;
     int xi = blockIdx.x * blockDim.x + threadIdx.x;
     int yi = blockIdx.y * blockDim.y + threadIdx.y;
     int z0 = blockIdx.z * ZPT;
@@ -148,8 +151,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
     // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
     // is only needed by the border recheck and is read from zpos there)
     const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
-    const size_t view_stride = (size_t)p.n_rows * p.nos;
-    const float p_max = (float)(p.nos - 2);
+    const size_t view_stride = (size_t)p.n_rows * nos;
+    const float p_max = (float)(nos - 2);
+    const float p_mid = 0.5f * p_max;
     const float q_max_last = (float)(p.n_rows - 2);
     const float z_end = fmaf((float)(ZPT - 1), p.coll, zbase);
     const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
@@ -157,6 +161,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
 
     for (int i = 0; i < p.n_half; ++i) {
         float s[ZPT], h[ZPT];
+        int n_flat = 0;  // flat visits of this angle: W = 1 for every slice
 #pragma unroll
         for (int z = 0; z < ZPT; ++z) {
             s[z] = 0.0f;
@@ -205,7 +210,10 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             if (q0 >= 1.0f || q_end <= -1.0f) continue;
             // p and its border decision exactly as the reference rounds them
             float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
-            if (fabsf(p_idx) < kBorderBand || fabsf(p_idx - p_max) < kBorderBand) p_idx = p_index_exact(p, phat);
+            // within the band of either border (|p_idx - p_mid| > p_mid - band; the
+            // fast p_idx is within 2e-4 of the exact one, the band is 1e-3):
+            // the exact p_idx decides, with the reference's own comparisons
+            if (fabsf(p_idx - p_mid) > p_mid - kBorderBand) p_idx = p_index_exact(p, phat);
             bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
             bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
@@ -222,21 +230,21 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             unsigned lanes = __activemask();
             if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
                 if (p_ok) {
+                    float ql0 = fmaf(q0, p.half_rows, p.half_rows);
+                    float dql = dq * p.half_rows;
 #pragma unroll
                     for (int z = 0; z < ZPT; ++z) {
-                        float q = fmaf((float)z, dq, q0);
-                        float ql = fmaf(q, p.half_rows, p.half_rows);
+                        float ql = fmaf((float)z, dql, ql0);
                         float row = floorf(ql);
                         float wq = ql - row;
                         float v00, v01, v10, v11;
-                        fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                        fetch_footprint(view, nos, row, v00, v01, v10, v11);
                         float c0 = fmaf(wp, v01 - v00, v00);
                         float c1 = fmaf(wp, v11 - v10, v10);
                         s[z] += fmaf(wq, c1 - c0, c0);
                     }
                 }
-#pragma unroll
-                for (int z = 0; z < ZPT; ++z) h[z] += 1.0f;
+                ++n_flat;
                 continue;
             }
             bool inner = a_max < kInnerMax && (!last || fmaf(a_max, p.half_rows, p.half_rows) < q_max_last - kRowMargin);
@@ -252,7 +260,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                         float row = floorf(ql);
                         float wq = ql - row;
                         float v00, v01, v10, v11;
-                        fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                        fetch_footprint(view, nos, row, v00, v01, v10, v11);
                         float c0 = fmaf(wp, v01 - v00, v00);
                         float c1 = fmaf(wp, v11 - v10, v10);
                         s[z] = fmaf(w, fmaf(wq, c1 - c0, c0), s[z]);
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                     float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
                     float wq = ql - row;
                     float v00, v01, v10, v11;
-                    fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                    fetch_footprint(view, nos, row, v00, v01, v10, v11);
                     bool ok = p_ok && in;
                     if (last && ok) {
                         float d = ql - q_max_last;
@@ -313,7 +321,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                 float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
                 float wq = ql - row;
                 float v00, v01, v10, v11;
-                fetch_footprint(view, p.nos, row, v00, v01, v10, v11);
+                fetch_footprint(view, nos, row, v00, v01, v10, v11);
                 float c0 = fmaf(wp, v01 - v00, v00);
                 float c1 = fmaf(wp, v11 - v10, v10);
                 s[z] = fmaf(p_ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
@@ -321,23 +329,15 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
         }
 #pragma unroll
         for (int z = 0; z < ZPT; ++z) {
-            float r = __fdividef(s[z], h[z]);
-            img[z * 256] += h[z] != 0.0f ? r : 0.0f;
+            float hz = h[z] + (float)n_flat;
+            float r = __fdividef(s[z], hz);
+            img[z * 256] += hz != 0.0f ? r : 0.0f;
         }
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
     for (int z = 0; z < ZPT; ++z)
         if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z * 256] * p.out_scale;
-}
-
-int bp_min_blocks()
-{
-    static int v = [] {
-        const char *e = getenv("CTBB_BP_MINB");
-        return e ? atoi(e) : 3;
-    }();
-    return v;
 }
 
 }  // namespace
@@ -430,8 +430,18 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
         constexpr int Z = decltype(zpt_tag)::value;
         grid.z = (p.n_slices + Z - 1) / Z;
         constexpr int MB = Z <= 8 ? 3 : 2;
-        if (Z == 8 && bp_min_blocks() == 4) backproject_kernel<8, 4><<<grid, block, 0, stream>>>(p);
-        else backproject_kernel<Z, MB><<<grid, block, 0, stream>>>(p);
+        if constexpr (Z == 8) {
+            // the row lengths of the built-in scanners with flying focal spot
+            if (p.nos == 1472) {
+                backproject_kernel<8, MB, 1472><<<grid, block, 0, stream>>>(p);
+                return;
+            }
+            if (p.nos == 1344) {
+                backproject_kernel<8, MB, 1344><<<grid, block, 0, stream>>>(p);
+                return;
+            }
+        }
+        backproject_kernel<Z, MB, 0><<<grid, block, 0, stream>>>(p);
     };
     switch (zpt) {
     case 16: go(std::integral_constant<int, 16>()); break;
