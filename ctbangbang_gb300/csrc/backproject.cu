@@ -127,6 +127,12 @@ __device__ __forceinline__ void fetch_footprint(const float *view, int nos, floa
     v11 = __ldg(r0 + nos + 1);
 }
 
+// Packed FP32 pairs (sm_100 family): one instruction for two lanes.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // NOS > 0: the row length as a compile-time constant (the second row of a
 // footprint is then an immediate offset); 0: taken from p.nos.
 template <int ZPT, int MIN_BLOCKS, int NOS>
@@ -160,12 +166,12 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
     const unsigned warp_lanes = __activemask();
 
     for (int i = 0; i < p.n_half; ++i) {
-        float s[ZPT], h[ZPT];
+        float2 s2[ZPT / 2], h2[ZPT / 2];  // per-angle sums of slice pairs
         int n_flat = 0;  // flat visits of this angle: W = 1 for every slice
 #pragma unroll
-        for (int z = 0; z < ZPT; ++z) {
-            s[z] = 0.0f;
-            h[z] = 0.0f;
+        for (int m = 0; m < ZPT / 2; ++m) {
+            s2[m] = make_float2(0.0f, 0.0f);
+            h2[m] = make_float2(0.0f, 0.0f);
         }
         // The views i + k n_half are half turns apart: p flips its sign from
         // one to the next and |p| stays, so asin(|p| / r_f) and sqrt(r_f^2 - p^2)
@@ -228,20 +234,41 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             //  other: per-slice validity, clamped rows, last-turn border.
             float a_max = fmaxf(fabsf(q0), fabsf(q_end));
             unsigned lanes = __activemask();
+            // Slices are processed in pairs (z, z + 1) with packed FP32
+            // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
+            // conversions and loads stay per slice.
+            const float2 wp2 = make_float2(wp, wp);
+            const float2 omwp2 = make_float2(1.0f - wp, 1.0f - wp);
+            const float2 dq2 = make_float2(dq, dq), q02 = make_float2(q0, q0);
+            const float2 hr2 = make_float2(p.half_rows, p.half_rows);
+            // bilinear value of a pair from its rows (clamped or not by the caller)
+            auto pair_value = [&](float2 ql, float2 row) -> float2 {
+                float2 wq = sub2(ql, row);
+                float a00, a01, a10, a11, b00, b01, b10, b11;
+                fetch_footprint(view, nos, row.x, a00, a01, a10, a11);
+                fetch_footprint(view, nos, row.y, b00, b01, b10, b11);
+                float2 c0 = fma2(wp2, make_float2(a01, b01), mul2(omwp2, make_float2(a00, b00)));
+                float2 c1 = fma2(wp2, make_float2(a11, b11), mul2(omwp2, make_float2(a10, b10)));
+                return fma2(wq, sub2(c1, c0), c0);
+            };
+            // cos^2 taper weight of a pair: W = 1 below Q (cos(0) = 1), then
+            // cos^2(pi/2 (|q| - Q) / (1 - Q))
+            auto pair_weight = [&](float2 q) -> float2 {
+                float2 t = make_float2(fmaxf(fabsf(q.x) - kQ, 0.0f), fmaxf(fabsf(q.y) - kQ, 0.0f));
+                float2 arg = mul2(t, make_float2(p.taper_scale, p.taper_scale));
+                float2 c = make_float2(__cosf(arg.x), __cosf(arg.y));
+                return mul2(c, c);
+            };
             if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
                 if (p_ok) {
                     float ql0 = fmaf(q0, p.half_rows, p.half_rows);
                     float dql = dq * p.half_rows;
+                    const float2 ql02 = make_float2(ql0, ql0), dql2 = make_float2(dql, dql);
 #pragma unroll
-                    for (int z = 0; z < ZPT; ++z) {
-                        float ql = fmaf((float)z, dql, ql0);
-                        float row = floorf(ql);
-                        float wq = ql - row;
-                        float v00, v01, v10, v11;
-                        fetch_footprint(view, nos, row, v00, v01, v10, v11);
-                        float c0 = fmaf(wp, v01 - v00, v00);
-                        float c1 = fmaf(wp, v11 - v10, v10);
-                        s[z] += fmaf(wq, c1 - c0, c0);
+                    for (int m = 0; m < ZPT / 2; ++m) {
+                        float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
+                        float2 row = make_float2(floorf(ql.x), floorf(ql.y));
+                        s2[m] = add2(s2[m], pair_value(ql, row));
                     }
                 }
                 ++n_flat;
@@ -251,26 +278,19 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             if (__all_sync(lanes, inner)) {
                 if (p_ok) {
 #pragma unroll
-                    for (int z = 0; z < ZPT; ++z) {
-                        float q = fmaf((float)z, dq, q0);
-                        float c = __cosf(fmaxf(fabsf(q) - kQ, 0.0f) * p.taper_scale);
-                        float w = c * c;
-                        h[z] += w;
-                        float ql = fmaf(q, p.half_rows, p.half_rows);
-                        float row = floorf(ql);
-                        float wq = ql - row;
-                        float v00, v01, v10, v11;
-                        fetch_footprint(view, nos, row, v00, v01, v10, v11);
-                        float c0 = fmaf(wp, v01 - v00, v00);
-                        float c1 = fmaf(wp, v11 - v10, v10);
-                        s[z] = fmaf(w, fmaf(wq, c1 - c0, c0), s[z]);
+                    for (int m = 0; m < ZPT / 2; ++m) {
+                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        float2 w = pair_weight(q);
+                        h2[m] = add2(h2[m], w);
+                        float2 ql = fma2(q, hr2, hr2);
+                        float2 row = make_float2(floorf(ql.x), floorf(ql.y));
+                        s2[m] = fma2(w, pair_value(ql, row), s2[m]);
                     }
                 } else {
 #pragma unroll
-                    for (int z = 0; z < ZPT; ++z) {
-                        float q = fmaf((float)z, dq, q0);
-                        float c = __cosf(fmaxf(fabsf(q) - kQ, 0.0f) * p.taper_scale);
-                        h[z] += c * c;
+                    for (int m = 0; m < ZPT / 2; ++m) {
+                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        h2[m] = add2(h2[m], pair_weight(q));
                     }
                 }
                 continue;
@@ -280,58 +300,58 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             // when p is off the detector) and validity only scales the weight, so
             // the loads of all slices can be issued together.  Only a warp with
             // a row near the last-turn border takes the per-slice border test.
+            const float row_max = (float)(p.n_rows - 2);
             bool border = last && fmaf(q_end, p.half_rows, p.half_rows) > q_max_last - kBorderBand;
             if (__any_sync(lanes, border)) {
 #pragma unroll
-                for (int z = 0; z < ZPT; ++z) {
-                    float q = fmaf((float)z, dq, q0);
-                    float aq = fabsf(q);
-                    bool in = aq < 1.0f;
-                    float c = __cosf(fmaxf(aq - kQ, 0.0f) * p.taper_scale);
-                    float w = in ? c * c : 0.0f;
-                    h[z] += w;
-                    float ql = fmaf(q, p.half_rows, p.half_rows);
-                    float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
-                    float wq = ql - row;
-                    float v00, v01, v10, v11;
-                    fetch_footprint(view, nos, row, v00, v01, v10, v11);
-                    bool ok = p_ok && in;
-                    if (last && ok) {
-                        float d = ql - q_max_last;
-                        if (d > kBorderBand) ok = false;
+                for (int m = 0; m < ZPT / 2; ++m) {
+                    float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                    bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
+                    float2 w = pair_weight(q);
+                    w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
+                    h2[m] = add2(h2[m], w);
+                    float2 ql = fma2(q, hr2, hr2);
+                    float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
+                                             fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
+                    float2 v = pair_value(ql, row);
+                    bool ok_x = p_ok && in_x, ok_y = p_ok && in_y;
+                    if (ok_x) {
+                        float d = ql.x - q_max_last;
+                        if (d > kBorderBand) ok_x = false;
                         else if (d > -kBorderBand)
-                            ok = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + z), k);
+                            ok_x = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + 2 * m), k);
                     }
-                    float c0 = fmaf(wp, v01 - v00, v00);
-                    float c1 = fmaf(wp, v11 - v10, v10);
-                    s[z] = fmaf(ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
+                    if (ok_y) {
+                        float d = ql.y - q_max_last;
+                        if (d > kBorderBand) ok_y = false;
+                        else if (d > -kBorderBand)
+                            ok_y = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat,
+                                                          __ldg(p.zpos + z0 + 2 * m + 1), k);
+                    }
+                    s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
                 }
                 continue;
             }
 #pragma unroll
-            for (int z = 0; z < ZPT; ++z) {
-                float q = fmaf((float)z, dq, q0);
-                float aq = fabsf(q);
-                bool in = aq < 1.0f;
-                // W = 1 below Q, cos^2 taper to |q| = 1 (cos(0) = 1 covers both)
-                float c = __cosf(fmaxf(aq - kQ, 0.0f) * p.taper_scale);
-                float w = in ? c * c : 0.0f;
-                h[z] += w;
-                float ql = fmaf(q, p.half_rows, p.half_rows);
-                float row = fminf(fmaxf(floorf(ql), 0.0f), (float)(p.n_rows - 2));
-                float wq = ql - row;
-                float v00, v01, v10, v11;
-                fetch_footprint(view, nos, row, v00, v01, v10, v11);
-                float c0 = fmaf(wp, v01 - v00, v00);
-                float c1 = fmaf(wp, v11 - v10, v10);
-                s[z] = fmaf(p_ok ? w : 0.0f, fmaf(wq, c1 - c0, c0), s[z]);
+            for (int m = 0; m < ZPT / 2; ++m) {
+                float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
+                float2 w = pair_weight(q);
+                w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
+                h2[m] = add2(h2[m], w);
+                float2 ql = fma2(q, hr2, hr2);
+                float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
+                                         fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
+                float2 v = pair_value(ql, row);
+                s2[m] = fma2(p_ok ? w : make_float2(0.0f, 0.0f), v, s2[m]);
             }
         }
 #pragma unroll
-        for (int z = 0; z < ZPT; ++z) {
-            float hz = h[z] + (float)n_flat;
-            float r = __fdividef(s[z], hz);
-            img[z * 256] += hz != 0.0f ? r : 0.0f;
+        for (int m = 0; m < ZPT / 2; ++m) {
+            float2 hz = add2(h2[m], make_float2((float)n_flat, (float)n_flat));
+            float rx = __fdividef(s2[m].x, hz.x), ry = __fdividef(s2[m].y, hz.y);
+            img[(2 * m) * 256] += hz.x != 0.0f ? rx : 0.0f;
+            img[(2 * m + 1) * 256] += hz.y != 0.0f ? ry : 0.0f;
         }
     }
     size_t plane = (size_t)p.nx * p.ny;
