@@ -48,6 +48,7 @@ def parse_args():
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-whole-scan", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="one block of the config through each stage once (small case for ncu captures)")
     return ap.parse_args()
@@ -405,6 +406,34 @@ def run_ours(args):
                "ms_per_step": e_ms, "matches_device_path": same}
         del h_scan, h_final
 
+    # the whole-scan path (one resident rebinned scan for all blocks) on the
+    # same resident scan, and how far its stack is from the block loop's
+    whole = None
+    if not args.no_whole_scan:
+        d_final2 = torch.empty_like(d_final)
+
+        def ws_step():
+            L.call("ctbb_reconstruct_scan_device", C.byref(mr), C.c_void_p(d_scan.data_ptr()),
+                   C.c_void_p(d_final2.data_ptr()), C.c_float(0.0))
+
+        for _ in range(max(args.warmup, 3)):
+            ws_step()
+        torch.cuda.synchronize()
+        w0 = torch.cuda.Event(enable_timing=True)
+        w1 = torch.cuda.Event(enable_timing=True)
+        w0.record()
+        for _ in range(args.steps):
+            ws_step()
+        w1.record()
+        torch.cuda.synchronize()
+        ws_ms = w0.elapsed_time(w1) / args.steps
+        diff = (d_final2 - d_final).double().abs()
+        hu = 1000.0 / scans.MU_WATER
+        whole = {"value": world * sizes["vu_total"] / (ws_ms * 1e-3), "unit": "voxel-updates/s",
+                 "ms_per_step": ws_ms, "max_hu_vs_block_loop": float(diff.max()) * hu,
+                 "rms_hu_vs_block_loop": float(diff.pow(2).mean().sqrt()) * hu,
+                 "entry_point": "ctbb_reconstruct_scan_device"}
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -465,6 +494,7 @@ def run_ours(args):
         "hbm_peak_gbs": hbm, "hbm_peak_kind": peak_kind,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "whole_scan": whole,
         "gpu_launches": launches / args.steps,
         "clocks": clk,
     }

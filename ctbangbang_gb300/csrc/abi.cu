@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -409,6 +410,86 @@ extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d
         CTBB_TRY(do_filter(*mr, c.rebin.as<float>()));
         float *slab = c.image.as<float>() + b * n_block * plane;
         CTBB_TRY(do_backproject(*mr, c.rebin.as<float>(), slab));
+    }
+    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), d_final, mu_water));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
+// Whole scan with one resident rebinned scan: the union of all blocks' pull
+// windows is adaptive-filtered, rebinned and ramp-filtered once, and every
+// block backprojects from its own offset into that rebinned scan (consecutive
+// windows overlap by most of their frames, which the block loop processes
+// again for every block).  Differs from the block loop only in the adaptive
+// filter's 18- and 180-degree statistics windows, which here are not cut at
+// the edges of each block's window.
+extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+                                            float mu_water)
+{
+    clear_error();
+    if (!mr || !d_scan || !d_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_scan_device: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+    const long long n_readings = (long long)mr->rp.n_readings;
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    const size_t n_block = mr->ri.n_slices_block;
+    // every block's plan, as the block loop makes them
+    std::vector<struct recon_info> blocks(mr->ri.n_blocks);
+    mr->ri.cb.block_idx = 0;
+    long long g0 = 0, g1 = 0;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        CTBB_TRY(plan_next_block(*mr, &blocks[b]));
+        mr->ri = blocks[b];
+        long long s0 = (long long)(int)blocks[b].idx_pull_start;
+        long long s1 = s0 + (long long)blocks[b].n_proj_pull;
+        g0 = b == 0 ? s0 : std::min(g0, s0);
+        g1 = b == 0 ? s1 : std::max(g1, s1);
+    }
+    if (blocks.empty()) return CTBB_OK;
+    const long long n_ffs = (long long)blocks[0].n_ffs;
+    for (const auto &ri : blocks)
+        if (((long long)(int)ri.idx_pull_start - g0) % n_ffs != 0) {
+            set_error("ctbb_reconstruct_scan_device: pull windows not aligned to the focal-spot cycle");
+            return CTBB_ERR_STATE;
+        }
+    // the union window as one "block"
+    struct recon_metadata mg = *mr;
+    mg.ri = blocks[0];
+    mg.ri.idx_pull_start = (size_t)g0;
+    mg.ri.n_proj_pull = (size_t)(g1 - g0);
+    BlockDims dg = block_dims(mg);
+    const float *d_win = nullptr;
+    if (g0 >= 0 && g1 <= n_readings) {
+        d_win = d_scan + (size_t)g0 * frame;
+    } else {
+        CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
+        CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, dg.raw_elems() * sizeof(float), c.stream));
+        long long a = g0 < 0 ? 0 : g0, e = g1 > n_readings ? n_readings : g1;
+        if (e > a)
+            CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - g0) * frame, d_scan + (size_t)a * frame,
+                                          (size_t)(e - a) * frame * sizeof(float), cudaMemcpyDeviceToDevice,
+                                          c.stream));
+        d_win = c.raw_in.as<float>();
+    }
+    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+    CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
+    CTBB_TRY(do_adaptive(mg, d_win, c.raw_filt.as<float>()));
+    CTBB_TRY(c.rebin.ensure(dg.rebin_elems() * sizeof(float)));
+    CTBB_TRY(do_rebin(mg, c.raw_filt.as<float>(), c.rebin.as<float>()));
+    CTBB_TRY(do_filter(mg, c.rebin.as<float>()));
+    const size_t view_elems = dg.n_rows * dg.n_os;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        mr->ri = blocks[b];
+        // view j of block b is view j + (pull_start_b - g0) / n_ffs of the union
+        size_t off = (size_t)(((long long)(int)blocks[b].idx_pull_start - g0) / n_ffs);
+        float *slab = c.image.as<float>() + b * n_block * plane;
+        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>() + off * view_elems, slab));
     }
     CTBB_TRY(do_finalize(*mr, c.image.as<float>(), d_final, mu_water));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));

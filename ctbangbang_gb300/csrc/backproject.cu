@@ -360,6 +360,16 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
         if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z * 256] * p.out_scale;
 }
 
+// CTAs per SM the backprojector is compiled for (3: 80 registers, 4: 64)
+int bp_min_blocks()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_MINB");
+        return e ? atoi(e) : 4;
+    }();
+    return v;
+}
+
 }  // namespace
 
 int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables *t)
@@ -452,6 +462,18 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
         constexpr int MB = Z <= 8 ? 3 : 2;
         if constexpr (Z == 8) {
             // the row lengths of the built-in scanners with flying focal spot
+            if (bp_min_blocks() == 4) {
+                if (p.nos == 1472) {
+                    backproject_kernel<8, 4, 1472><<<grid, block, 0, stream>>>(p);
+                    return;
+                }
+                if (p.nos == 1344) {
+                    backproject_kernel<8, 4, 1344><<<grid, block, 0, stream>>>(p);
+                    return;
+                }
+                backproject_kernel<8, 4, 0><<<grid, block, 0, stream>>>(p);
+                return;
+            }
             if (p.nos == 1472) {
                 backproject_kernel<8, MB, 1472><<<grid, block, 0, stream>>>(p);
                 return;

@@ -339,6 +339,19 @@ int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image,
 int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
                             float *d_final, float mu_water);
 
+/* Whole scan from one resident rebinned scan (no counterpart in the
+   reference, whose block loop pulls, filters and rebins each block's window
+   separately although consecutive windows share most of their frames): the
+   union of all blocks' pull windows is adaptive-filtered, rebinned and
+   ramp-filtered once, and each block is backprojected from its offset into
+   it.  Same plan, block order and output as ctbb_reconstruct_device; the one
+   difference is that the adaptive filter's 18- and 180-degree statistics
+   windows run over the union instead of stopping at each block's window
+   edges, so the images differ where that filter acts near those edges.
+   Device memory: the union window's filtered raw data and rebinned rows. */
+int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan,
+                                 float *d_final, float mu_water);
+
 /* As ctbb_reconstruct_device from host buffers: each block's pull window is
    copied from h_scan [n_readings][n_rows_raw][n_channels] on a second stream
    (double-buffered, overlapping the previous block's compute when h_scan is
