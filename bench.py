@@ -3,17 +3,23 @@
 A step is one full reconstruction of the config-2 scan (736 channels x 32
 raw rows, phi+z flying focal spot rebinned to 1472 x 64, 1152 views/turn,
 pitch 0.8, 10 turns, 512^2 x 96 raw slices in 3 blocks of 32, thickened to
-16 final 3 mm slices): per block adaptive raw filter -> FFS rebin -> ramp
-filter -> FP32 wFBP backprojection, then reorder/thicken.  Input: a seeded
-synthetic phantom scan (water cylinder + 30 ellipsoids, Poisson noise at
-I0 = 5e4) generated on the device; there is no public dataset.
+16 final 3 mm slices): adaptive raw filter -> FFS rebin -> ramp filter ->
+FP32 wFBP backprojection of every block, then reorder/thicken.  Input: a
+seeded synthetic phantom scan (water cylinder + 30 ellipsoids, Poisson noise
+at I0 = 5e4) generated on the device; there is no public dataset.
+
+--path scan (default) runs the whole-scan entry points: the union of the
+blocks' pull windows is filtered and rebinned once and every block is
+backprojected from it.  --path blocks runs the reference's block loop (each
+block's window filtered and rebinned on its own).  The line reports the other
+path too ("other_path") with the HU difference between the two stacks.
 
   value  voxel-updates/s with the raw scan resident in HBM (device-timed with
-         CUDA events on the library's stream); 4.3 GB of raw input per step is
-         larger than L2, so no flush is needed between steps.
-  e2e    the same metric through ctbb_reconstruct_host from pinned host
-         buffers: each block's pull window is copied host->device and the final
-         stack device->host inside the timed region.
+         CUDA events on the library's stream); each step reads over 2 GB of
+         raw input, more than L2, so no flush is needed between steps.
+  e2e    the same metric through the host-buffer entry point from pinned host
+         buffers: the raw frames are copied host->device and the final stack
+         device->host inside the timed region.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -48,7 +54,11 @@ def parse_args():
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-whole-scan", action="store_true")
+    ap.add_argument("--no-whole-scan", action="store_true",
+                    help="skip the measurement of the other path (see --path)")
+    ap.add_argument("--path", choices=["scan", "blocks"], default="scan",
+                    help="scan: one resident rebinned scan for all blocks (ctbb_reconstruct_scan_*); "
+                         "blocks: the reference's block loop (ctbb_reconstruct_device / _host)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one block of the config through each stage once (small case for ncu captures)")
     return ap.parse_args()
@@ -93,12 +103,17 @@ def workload_sizes(mr, blocks):
     frame = mr.cg.n_rows_raw * mr.cg.n_channels
     n_readings = mr.rp.n_readings
     h2d = 0
+    g0 = g1 = None
     for ri in blocks:
         s = int(ri.idx_pull_start)
         s = s - 2 ** 64 if s >= 2 ** 63 else s
         a, e = max(s, 0), min(s + ri.n_proj_pull, n_readings)
         h2d += max(e - a, 0) * frame * 4
+        g0 = s if g0 is None else min(g0, s)
+        g1 = s + ri.n_proj_pull if g1 is None else max(g1, s + ri.n_proj_pull)
+    union_h2d = max(min(g1, n_readings) - max(g0, 0), 0) * frame * 4
     return dict(nht=nht, vu_per_block=vu_blocks, vu_total=sum(vu_blocks), h2d_bytes=h2d,
+                union_h2d_bytes=union_h2d,
                 raw_samples=[ri.n_proj_pull * frame for ri in blocks],
                 rebin_samples=[(ri.n_proj_pull // ri.n_ffs - 2 * mr.cg.add_projections) * mr.cg.n_rows *
                                mr.cg.n_channels_oversampled for ri in blocks])
@@ -336,8 +351,15 @@ def run_ours(args):
            C.c_void_p(d_scan.data_ptr()))
     d_final = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
 
+    entry = {"scan": ("ctbb_reconstruct_scan_device", "ctbb_reconstruct_scan_host"),
+             "blocks": ("ctbb_reconstruct_device", "ctbb_reconstruct_host")}
+    other_path = "blocks" if args.path == "scan" else "scan"
+    dev_entry, host_entry = entry[args.path]
+    alt_dev, alt_host = entry[other_path]
+    h2d_key = {"scan": "union_h2d_bytes", "blocks": "h2d_bytes"}
+
     def step():
-        L.call("ctbb_reconstruct_device", C.byref(mr), C.c_void_p(d_scan.data_ptr()),
+        L.call(dev_entry, C.byref(mr), C.c_void_p(d_scan.data_ptr()),
                C.c_void_p(d_final.data_ptr()), C.c_float(0.0))
 
     for _ in range(max(args.warmup, 3)):
@@ -376,6 +398,7 @@ def run_ours(args):
 
     # e2e through the host-buffer entry point (pinned host scan and stack)
     e2e = None
+    ws_e2e = None
     if not args.no_e2e:
         h_scan = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
         h_scan.copy_(d_scan)
@@ -384,7 +407,7 @@ def run_ours(args):
         fp = h_final.numpy().ctypes.data_as(C.POINTER(C.c_float))
 
         def e2e_step():
-            L.call("ctbb_reconstruct_host", C.byref(mr), hp, fp, C.c_float(0.0))
+            L.call(host_entry, C.byref(mr), hp, fp, C.c_float(0.0))
 
         for _ in range(2):
             e2e_step()
@@ -402,18 +425,40 @@ def run_ours(args):
             e_ms = float(t.item())
         same = bool(torch.equal(h_final.cuda(), d_final))
         e2e = {"value": world * sizes["vu_total"] / (e_ms * 1e-3), "unit": "voxel-updates/s",
-               "h2d_bytes_per_step": sizes["h2d_bytes"], "d2h_bytes_per_step": n_final * plane * 4,
-               "ms_per_step": e_ms, "matches_device_path": same}
+               "h2d_bytes_per_step": sizes[h2d_key[args.path]], "d2h_bytes_per_step": n_final * plane * 4,
+               "ms_per_step": e_ms, "matches_device_path": same, "entry_point": host_entry}
+        if not args.no_whole_scan:
+            # the other path from the same pinned buffers
+            def ws_host_step():
+                L.call(alt_host, C.byref(mr), hp, fp, C.c_float(0.0))
+
+            for _ in range(2):
+                ws_host_step()
+            if dist is not None:
+                dist.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ws_host_step()
+            torch.cuda.synchronize()
+            ws_e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+            if dist is not None:
+                t = torch.tensor([ws_e_ms], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                ws_e_ms = float(t.item())
+            ws_e2e = {"value": world * sizes["vu_total"] / (ws_e_ms * 1e-3), "unit": "voxel-updates/s",
+                      "h2d_bytes_per_step": sizes[h2d_key[other_path]], "d2h_bytes_per_step": n_final * plane * 4,
+                      "ms_per_step": ws_e_ms, "entry_point": alt_host}
         del h_scan, h_final
 
-    # the whole-scan path (one resident rebinned scan for all blocks) on the
-    # same resident scan, and how far its stack is from the block loop's
+    # the other path (block loop or whole scan) on the same resident scan, and
+    # how far its stack is from this path's
     whole = None
     if not args.no_whole_scan:
         d_final2 = torch.empty_like(d_final)
 
         def ws_step():
-            L.call("ctbb_reconstruct_scan_device", C.byref(mr), C.c_void_p(d_scan.data_ptr()),
+            L.call(alt_dev, C.byref(mr), C.c_void_p(d_scan.data_ptr()),
                    C.c_void_p(d_final2.data_ptr()), C.c_float(0.0))
 
         for _ in range(max(args.warmup, 3)):
@@ -429,10 +474,11 @@ def run_ours(args):
         ws_ms = w0.elapsed_time(w1) / args.steps
         diff = (d_final2 - d_final).double().abs()
         hu = 1000.0 / scans.MU_WATER
-        whole = {"value": world * sizes["vu_total"] / (ws_ms * 1e-3), "unit": "voxel-updates/s",
-                 "ms_per_step": ws_ms, "max_hu_vs_block_loop": float(diff.max()) * hu,
-                 "rms_hu_vs_block_loop": float(diff.pow(2).mean().sqrt()) * hu,
-                 "entry_point": "ctbb_reconstruct_scan_device"}
+        whole = {"path": other_path, "value": world * sizes["vu_total"] / (ws_ms * 1e-3),
+                 "unit": "voxel-updates/s", "ms_per_step": ws_ms,
+                 "max_hu_between_paths": float(diff.max()) * hu,
+                 "rms_hu_between_paths": float(diff.pow(2).mean().sqrt()) * hu,
+                 "entry_point": alt_dev, "e2e": ws_e2e}
 
     if rank != 0:
         if dist is not None:
@@ -477,11 +523,16 @@ def run_ours(args):
         "config": {
             "workload": "%s: 736 ch x 32 rows phi+z FFS -> 1472 x 64, 1152 views/turn, pitch 0.8, 10 turns, "
                         "512^2 x 96 slices (3 blocks) thickened to %d x 3 mm; adaptive filter on" % (args.config, n_final),
+            "path": ("whole scan: the union of the blocks' pull windows (%d frames) adaptive-filtered, rebinned "
+                     "and ramp-filtered once, each block backprojected from it (%s / %s)"
+                     % (sizes["union_h2d_bytes"] // (4 * frame), dev_entry, host_entry)) if args.path == "scan" else
+                    ("block loop as the reference: each block's pull window filtered, rebinned and backprojected "
+                     "(%s / %s)" % (dev_entry, host_entry)),
             "scans_per_s": world / (ms * 1e-3),
             "voxel_updates_per_scan": sizes["vu_total"],
             "latency_ms": {"p50": per_step_sorted[len(per_step) // 2],
                            "p99": per_step_sorted[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]},
-            "l2": "no flush: each step reads a 4.3 GB raw scan (> 129 MB L2)",
+            "l2": "no flush: each step reads %.1f GB of raw frames (> 129 MB L2)" % (sizes[h2d_key[args.path]] / 1e9),
             "parallelism": "replicas" if world > 1 else "single GPU",
         },
         "roofline": {"kernel": "backproject_kernel", "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
@@ -494,7 +545,7 @@ def run_ours(args):
         "hbm_peak_gbs": hbm, "hbm_peak_kind": peak_kind,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "whole_scan": whole,
+        "other_path": whole,
         "gpu_launches": launches / args.steps,
         "clocks": clk,
     }

@@ -73,6 +73,7 @@ struct Context {
     DeviceBuffer raw_in2;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> chunk_copied;  // whole-scan host path: one per chunk
     // per-stage CUDA-event timing (ctbb_profile_*)
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> open_events[kProfileStages];
@@ -144,6 +145,17 @@ int check_mr(const struct recon_metadata *mr)
         return CTBB_ERR_STATE;
     }
     return CTBB_OK;
+}
+
+// Chunks the whole-scan host path copies the union window in.
+int scan_chunks()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_SCAN_CHUNKS");
+        int n = e ? atoi(e) : 8;
+        return n < 1 ? 1 : (n > 64 ? 64 : n);
+    }();
+    return v;
 }
 
 // Default voxels-per-thread of the backprojector along z.
@@ -416,6 +428,47 @@ extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d
     return CTBB_OK;
 }
 
+// Every block's plan, as the block loop makes them, and the union of their
+// pull windows [g0, g1) as one plan mg (the whole-scan paths).
+static int plan_union(struct recon_metadata *mr, std::vector<struct recon_info> *blocks, long long *g0_out,
+                      long long *g1_out, struct recon_metadata *mg)
+{
+    blocks->assign(mr->ri.n_blocks, recon_info{});
+    mr->ri.cb.block_idx = 0;
+    long long g0 = 0, g1 = 0;
+    for (size_t b = 0; b < blocks->size(); ++b) {
+        CTBB_TRY(plan_next_block(*mr, &(*blocks)[b]));
+        mr->ri = (*blocks)[b];
+        long long s0 = (long long)(int)(*blocks)[b].idx_pull_start;
+        long long s1 = s0 + (long long)(*blocks)[b].n_proj_pull;
+        g0 = b == 0 ? s0 : std::min(g0, s0);
+        g1 = b == 0 ? s1 : std::max(g1, s1);
+    }
+    if (blocks->empty()) {
+        set_error("whole scan: the plan has no blocks");
+        return CTBB_ERR_STATE;
+    }
+    const long long n_ffs = (long long)(*blocks)[0].n_ffs;
+    for (const auto &ri : *blocks)
+        if (((long long)(int)ri.idx_pull_start - g0) % n_ffs != 0) {
+            set_error("whole scan: pull windows not aligned to the focal-spot cycle");
+            return CTBB_ERR_STATE;
+        }
+    *mg = *mr;
+    mg->ri = (*blocks)[0];
+    mg->ri.idx_pull_start = (size_t)g0;
+    mg->ri.n_proj_pull = (size_t)(g1 - g0);
+    *g0_out = g0;
+    *g1_out = g1;
+    return CTBB_OK;
+}
+
+// first rebinned view of block b in the union's rebinned rows
+static size_t union_view_offset(const struct recon_info &ri, long long g0)
+{
+    return (size_t)(((long long)(int)ri.idx_pull_start - g0) / (long long)ri.n_ffs);
+}
+
 // Whole scan with one resident rebinned scan: the union of all blocks' pull
 // windows is adaptive-filtered, rebinned and ramp-filtered once, and every
 // block backprojects from its own offset into that rebinned scan (consecutive
@@ -439,30 +492,10 @@ extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const flo
     const long long n_readings = (long long)mr->rp.n_readings;
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     const size_t n_block = mr->ri.n_slices_block;
-    // every block's plan, as the block loop makes them
-    std::vector<struct recon_info> blocks(mr->ri.n_blocks);
-    mr->ri.cb.block_idx = 0;
+    std::vector<struct recon_info> blocks;
     long long g0 = 0, g1 = 0;
-    for (size_t b = 0; b < blocks.size(); ++b) {
-        CTBB_TRY(plan_next_block(*mr, &blocks[b]));
-        mr->ri = blocks[b];
-        long long s0 = (long long)(int)blocks[b].idx_pull_start;
-        long long s1 = s0 + (long long)blocks[b].n_proj_pull;
-        g0 = b == 0 ? s0 : std::min(g0, s0);
-        g1 = b == 0 ? s1 : std::max(g1, s1);
-    }
-    if (blocks.empty()) return CTBB_OK;
-    const long long n_ffs = (long long)blocks[0].n_ffs;
-    for (const auto &ri : blocks)
-        if (((long long)(int)ri.idx_pull_start - g0) % n_ffs != 0) {
-            set_error("ctbb_reconstruct_scan_device: pull windows not aligned to the focal-spot cycle");
-            return CTBB_ERR_STATE;
-        }
-    // the union window as one "block"
-    struct recon_metadata mg = *mr;
-    mg.ri = blocks[0];
-    mg.ri.idx_pull_start = (size_t)g0;
-    mg.ri.n_proj_pull = (size_t)(g1 - g0);
+    struct recon_metadata mg;
+    CTBB_TRY(plan_union(mr, &blocks, &g0, &g1, &mg));
     BlockDims dg = block_dims(mg);
     const float *d_win = nullptr;
     if (g0 >= 0 && g1 <= n_readings) {
@@ -487,7 +520,7 @@ extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const flo
     for (size_t b = 0; b < blocks.size(); ++b) {
         mr->ri = blocks[b];
         // view j of block b is view j + (pull_start_b - g0) / n_ffs of the union
-        size_t off = (size_t)(((long long)(int)blocks[b].idx_pull_start - g0) / n_ffs);
+        size_t off = union_view_offset(blocks[b], g0);
         float *slab = c.image.as<float>() + b * n_block * plane;
         CTBB_TRY(do_backproject(*mr, c.rebin.as<float>() + off * view_elems, slab));
     }
@@ -634,6 +667,153 @@ int finalize_image_stack(struct recon_metadata *mr) { return ctbb_finalize_image
 // whole scan from host buffers
 // --------------------------------------------------------------------------
 
+// the copy stream and the double-buffer events of the host block loop
+static int ensure_copy_stream(Context &c)
+{
+    if (c.copy_stream) return CTBB_OK;
+    CTBB_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
+        CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.consumed[i], cudaEventDisableTiming));
+        CTBB_CUDA_TRY(cudaEventRecord(c.consumed[i], c.copy_stream));
+    }
+    return CTBB_OK;
+}
+
+// Whole scan from host buffers, streamed: the union window is copied in
+// chunks on the copy stream while, on the compute stream, each arriving chunk
+// advances the adaptive filter as far as its statistics windows allow, the
+// views whose frames are final are rebinned and ramp-filtered, and every
+// block whose views are all ready is backprojected.  Same kernels on the same
+// data as ctbb_reconstruct_scan_device, so the same result.
+extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                                          float mu_water)
+{
+    clear_error();
+    if (!mr || !h_scan || !h_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_scan_host: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    CTBB_TRY(ensure_copy_stream(c));
+    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+    const long long n_readings = (long long)mr->rp.n_readings;
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    const size_t n_block = mr->ri.n_slices_block;
+    std::vector<struct recon_info> blocks;
+    long long g0 = 0, g1 = 0;
+    struct recon_metadata mg;
+    CTBB_TRY(plan_union(mr, &blocks, &g0, &g1, &mg));
+    BlockDims dg = block_dims(mg);
+    const int G = (int)(g1 - g0);
+    int n_final = ctbb_n_slices_final(mr);
+    CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
+    CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
+    CTBB_TRY(c.rebin.ensure(dg.rebin_elems() * sizeof(float)));
+    CTBB_TRY(c.scratch.ensure(adaptive_filter_scratch_floats(dg.n_proj_pull) * sizeof(float)));
+    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+    CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
+    // the union window in chunks of whole focal-spot cycles; the copy stream
+    // starts once the compute stream has finished with the buffer
+    const int n_ffs = (int)dg.n_ffs;
+    int chunk = (G + scan_chunks() - 1) / scan_chunks();
+    chunk = ((chunk + n_ffs - 1) / n_ffs) * n_ffs;
+    const int n_chunks = (G + chunk - 1) / chunk;
+    while ((int)c.chunk_copied.size() < n_chunks) {
+        cudaEvent_t e;
+        CTBB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c.chunk_copied.push_back(e);
+    }
+    CTBB_CUDA_TRY(cudaEventRecord(c.consumed[0], c.stream));
+    CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[0], 0));
+    float *d_raw = c.raw_in.as<float>();
+    for (int k = 0; k < n_chunks; ++k) {
+        long long a = g0 + (long long)k * chunk, e = std::min(g1, a + chunk);
+        long long da = std::max(a, 0LL), de = std::min(e, n_readings);
+        float *dst = d_raw + (size_t)(a - g0) * frame;
+        if (de <= da) {
+            CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(e - a) * frame * sizeof(float), c.copy_stream));
+        } else {
+            if (da > a) CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(da - a) * frame * sizeof(float), c.copy_stream));
+            CTBB_CUDA_TRY(cudaMemcpyAsync(d_raw + (size_t)(da - g0) * frame, h_scan + (size_t)da * frame,
+                                          (size_t)(de - da) * frame * sizeof(float), cudaMemcpyHostToDevice,
+                                          c.copy_stream));
+            if (e > de)
+                CTBB_CUDA_TRY(cudaMemsetAsync(d_raw + (size_t)(de - g0) * frame, 0,
+                                              (size_t)(e - de) * frame * sizeof(float), c.copy_stream));
+        }
+        CTBB_CUDA_TRY(cudaEventRecord(c.chunk_copied[k], c.copy_stream));
+    }
+    // per-scan tables, once
+    RebinTables rt;
+    CTBB_TRY(build_rebin_tables(mg, &rt));
+    CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
+    {
+        std::vector<float> taps(2 * dg.n_os);
+        CTBB_TRY(ctbb_load_filter(&mg, taps.data()));
+        CTBB_TRY(prepare_ramp_filter(taps.data(), (int)dg.n_os, &c.ramp, c.stream));
+    }
+    AfStream af(mg);
+    const size_t view_elems = dg.n_rows * dg.n_os;
+    const int V = (int)dg.n_views;
+    int v_done = 0;
+    size_t b_done = 0;
+    for (int k = 0; k < n_chunks; ++k) {
+        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.chunk_copied[k], 0));
+        int arrived = std::min(G, (k + 1) * chunk);
+        {
+            StageScope scope(c, 0);
+            CTBB_TRY(af.advance(mg, d_raw, c.raw_filt.as<float>(), c.scratch.as<float>(), arrived, c.stream));
+        }
+        // views whose frames are all final
+        int v_ready = V;
+        if (af.filtered() < G) {
+            v_ready = 0;
+            while (v_ready < V && rebin_frames_needed(rt, v_ready) <= af.filtered()) ++v_ready;
+        }
+        if (v_ready > v_done) {
+            {
+                StageScope scope(c, 1);
+                CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream,
+                                      v_done, v_ready));
+            }
+            {
+                StageScope scope(c, 2);
+                CTBB_TRY(launch_ramp_filter(c.ramp, c.rebin.as<float>() + (size_t)v_done * view_elems,
+                                            (size_t)(v_ready - v_done) * dg.n_rows, c.stream));
+            }
+            v_done = v_ready;
+        }
+        // blocks whose views (i + k n_half, k < nht) are all ready
+        while (b_done < blocks.size()) {
+            struct recon_metadata mb = *mr;
+            mb.ri = blocks[b_done];
+            BlockDims db = block_dims(mb);
+            size_t need = union_view_offset(blocks[b_done], g0) +
+                          (size_t)db.n_half_turns * (size_t)(mr->cg.n_proj_turn / 2);
+            if (need > (size_t)v_done && v_done < V) break;
+            mr->ri = blocks[b_done];
+            float *slab = c.image.as<float>() + b_done * n_block * plane;
+            CTBB_TRY(do_backproject(*mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
+                                    slab));
+            ++b_done;
+        }
+    }
+    if (b_done != blocks.size()) {
+        set_error("ctbb_reconstruct_scan_host: %zu of %zu blocks left unfinished", blocks.size() - b_done,
+                  blocks.size());
+        return CTBB_ERR_STATE;
+    }
+    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
+                                  cudaMemcpyDeviceToHost, c.stream));
+    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return CTBB_OK;
+}
+
 extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
                                      float mu_water)
 {
@@ -646,14 +826,7 @@ extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_s
     CTBB_TRY(require_device());
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
-    if (!c.copy_stream) {
-        CTBB_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
-        for (int i = 0; i < 2; ++i) {
-            CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
-            CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.consumed[i], cudaEventDisableTiming));
-            CTBB_CUDA_TRY(cudaEventRecord(c.consumed[i], c.copy_stream));
-        }
-    }
+    CTBB_TRY(ensure_copy_stream(c));
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const long long n_readings = mr->rp.n_readings;
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;

@@ -25,6 +25,7 @@
 // (rows of a multiple of 4 channels; otherwise a shared-memory tiled stencil).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -52,11 +53,12 @@ struct AfParams {
     int n_avg, avg_offset;
     int n_range, range_offset;
     float strength;
+    int f0, f1;  // frames this launch writes: [f0, f1) of the window [0, P)
 };
 
 __global__ void af_sup_kernel(AfParams p)
 {
-    int proj = blockIdx.x;
+    int proj = p.f0 + blockIdx.x;
     size_t frame = (size_t)p.R * p.N;
     const float *src = p.raw + (size_t)proj * frame;
     float m = 0.0f;
@@ -82,8 +84,8 @@ __global__ void af_sup_kernel(AfParams p)
 
 __global__ void af_smooth_kernel(AfParams p)
 {
-    int proj = blockIdx.x * blockDim.x + threadIdx.x;
-    if (proj >= p.P) return;
+    int proj = p.f0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (proj >= p.f1) return;
     float w = __fdiv_rn(1.0f, (float)p.n_avg);
     float acc = 0.0f;
     int max_idx = p.P - 1;
@@ -97,8 +99,8 @@ __global__ void af_smooth_kernel(AfParams p)
 
 __global__ void af_ecc_kernel(AfParams p)
 {
-    int proj = blockIdx.x * blockDim.x + threadIdx.x;
-    if (proj >= p.P) return;
+    int proj = p.f0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (proj >= p.f1) return;
     int max_idx = p.P - 1;
     float vmax = 0.0f, vmin = 10000.0f;
     for (int i = 0; i < p.n_range; i++) {
@@ -141,8 +143,8 @@ __global__ void af_threshold_kernel(AfParams p)
 {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
-    if (warp >= p.P) return;
-    int proj = warp;
+    int proj = p.f0 + warp;
+    if (proj >= p.f1) return;
     float lower = p.pmin[proj];
     float upper = p.pmax[proj];
     float T = __fdiv_rn(__fadd_rn(p.pmax[proj], p.pmin[proj]), 2.0f);
@@ -170,7 +172,7 @@ constexpr int SP = TP + 4, SR = TR + 4, SC = TC + 4;
 __global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
 {
     __shared__ float tile[SP][SR][SC];
-    int c0 = blockIdx.x * TC, r0 = blockIdx.y * TR, p0 = blockIdx.z * TP;
+    int c0 = blockIdx.x * TC, r0 = blockIdx.y * TR, p0 = p.f0 + blockIdx.z * TP;
     size_t frame = (size_t)p.R * p.N;
     for (int t = threadIdx.x; t < SP * SR * SC; t += blockDim.x) {
         int sc = t % SC, sr = (t / SC) % SR, sp = t / (SC * SR);
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(256) af_filter_kernel(AfParams p)
     for (int t = threadIdx.x; t < TP * TR * TC; t += blockDim.x) {
         int lc = t % TC, lr = (t / TC) % TR, lp = t / (TC * TR);
         int gc = c0 + lc, gr = r0 + lr, gp = p0 + lp;
-        if (gc >= p.N || gr >= p.R || gp >= p.P) continue;
+        if (gc >= p.N || gr >= p.R || gp >= p.f1) continue;
         float x = tile[lp + 2][lr + 2][lc + 2];
         float T = p.thr[gp];
         float y = x;
@@ -253,7 +255,7 @@ __device__ __noinline__ float smooth_sample(const AfParams &p, int gp, int gr, i
 // kernel runs at copy speed.  Same arithmetic, same result as the tiled form.
 __global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
 {
-    int gp = blockIdx.x;
+    int gp = p.f0 + blockIdx.x;
     size_t frame = (size_t)p.R * p.N;
     const float4 *src = reinterpret_cast<const float4 *>(p.raw + (size_t)gp * frame);
     float4 *dst = reinterpret_cast<float4 *>(p.out + (size_t)gp * frame);
@@ -278,10 +280,11 @@ __global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
 
 size_t adaptive_filter_scratch_floats(size_t n_proj_pull) { return 6 * n_proj_pull; }
 
-int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
-                           float *d_scratch, cudaStream_t stream)
+namespace {
+
+int af_params(const struct recon_metadata &mr, const float *d_in, float *d_out, float *d_scratch, AfParams *pp)
 {
-    AfParams p;
+    AfParams &p = *pp;
     p.raw = d_in;
     p.out = d_out;
     p.P = (int)mr.ri.n_proj_pull;
@@ -304,26 +307,96 @@ int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, f
     p.n_range = n_range;
     p.range_offset = (int)floorf((float)(n_range / 2));
     p.strength = mr.rp.adaptive_filtration_s;
+    p.f0 = 0;
+    p.f1 = p.P;
     if (p.P <= 0 || p.R <= 0 || p.N <= 0) {
         set_error("adaptive filter: empty pull window");
         return CTBB_ERR_ARGUMENT;
     }
-    af_sup_kernel<<<p.P, 256, 0, stream>>>(p);
-    af_smooth_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
-    af_ecc_kernel<<<(p.P + 127) / 128, 128, 0, stream>>>(p);
-    af_threshold_kernel<<<(p.P * 32 + 255) / 256, 256, 0, stream>>>(p);
-    if (p.N % 4 == 0) {
-        af_filter_stream_kernel<<<p.P, 256, 0, stream>>>(p);
-    } else {
-        dim3 grid((p.N + TC - 1) / TC, (p.R + TR - 1) / TR, (p.P + TP - 1) / TP);
-        if (grid.z > 65535) {
-            set_error("adaptive filter: %d frames exceed the launch grid", p.P);
-            return CTBB_ERR_ARGUMENT;
-        }
-        af_filter_kernel<<<grid, 256, 0, stream>>>(p);
+    return CTBB_OK;
+}
+
+// The five steps over frame ranges: maxima of [sup0, sup1), moving means of
+// [smooth0, smooth1), eccentricity, threshold and smoothing of [out0, out1).
+// Each range may be empty; a step reads the earlier steps' results of the
+// frames its windows cover, which the caller has launched before.
+int af_launch(AfParams p, int sup0, int sup1, int smooth0, int smooth1, int out0, int out1, cudaStream_t stream)
+{
+    int launches = 0;
+    if (sup1 > sup0) {
+        p.f0 = sup0;
+        p.f1 = sup1;
+        af_sup_kernel<<<sup1 - sup0, 256, 0, stream>>>(p);
+        ++launches;
     }
-    count_launch(5);
+    if (smooth1 > smooth0) {
+        p.f0 = smooth0;
+        p.f1 = smooth1;
+        af_smooth_kernel<<<(smooth1 - smooth0 + 127) / 128, 128, 0, stream>>>(p);
+        ++launches;
+    }
+    if (out1 > out0) {
+        int n = out1 - out0;
+        p.f0 = out0;
+        p.f1 = out1;
+        af_ecc_kernel<<<(n + 127) / 128, 128, 0, stream>>>(p);
+        af_threshold_kernel<<<(n * 32 + 255) / 256, 256, 0, stream>>>(p);
+        if (p.N % 4 == 0) {
+            af_filter_stream_kernel<<<n, 256, 0, stream>>>(p);
+        } else {
+            dim3 grid((p.N + TC - 1) / TC, (p.R + TR - 1) / TR, (n + TP - 1) / TP);
+            if (grid.z > 65535) {
+                set_error("adaptive filter: %d frames exceed the launch grid", n);
+                return CTBB_ERR_ARGUMENT;
+            }
+            af_filter_kernel<<<grid, 256, 0, stream>>>(p);
+        }
+        launches += 3;
+    }
+    count_launch(launches);
     CTBB_CUDA_TRY(cudaGetLastError());
+    return CTBB_OK;
+}
+
+}  // namespace
+
+int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                           float *d_scratch, cudaStream_t stream)
+{
+    AfParams p;
+    CTBB_TRY(af_params(mr, d_in, d_out, d_scratch, &p));
+    return af_launch(p, 0, p.P, 0, p.P, 0, p.P, stream);
+}
+
+AfStream::AfStream(const struct recon_metadata &mr) : P((int)mr.ri.n_proj_pull)
+{
+    int n_proj_ffs = (int)mr.cg.n_proj_ffs;
+    int n_avg = (int)ceilf((18.0f / 360.0f) * (float)n_proj_ffs);
+    n_avg = n_avg + (1 - n_avg % 2);
+    int n_range = (int)ceilf((180.0f / 360.0f) * (float)n_proj_ffs);
+    n_range = n_range + (1 - n_range % 2);
+    avg_reach = n_avg / 2;
+    range_reach = n_range / 2;
+}
+
+int AfStream::advance(const struct recon_metadata &mr, const float *d_in, float *d_out, float *d_scratch,
+                      int arrived, cudaStream_t stream)
+{
+    AfParams p;
+    CTBB_TRY(af_params(mr, d_in, d_out, d_scratch, &p));
+    arrived = std::min(arrived, P);
+    bool all = arrived == P;
+    // a moving mean needs the maxima up to avg_reach frames ahead, the
+    // eccentricity and threshold the means up to range_reach ahead, the
+    // smoothing the thresholds and raw frames of +-2 frames
+    int smoothed = all ? P : std::max(0, arrived - avg_reach);
+    int finished = all ? P : std::max(0, std::min(smoothed - range_reach, arrived - 2));
+    smoothed = std::max(smoothed, n_smoothed);
+    finished = std::max(finished, n_filtered);
+    CTBB_TRY(af_launch(p, n_sup, arrived, n_smoothed, smoothed, n_filtered, finished, stream));
+    n_sup = std::max(n_sup, arrived);
+    n_smoothed = smoothed;
+    n_filtered = finished;
     return CTBB_OK;
 }
 

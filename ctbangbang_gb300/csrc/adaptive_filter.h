@@ -15,4 +15,19 @@ size_t adaptive_filter_scratch_floats(size_t n_proj_pull);
 int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
                            float *d_scratch, cudaStream_t stream);
 
+// The same filter over a window whose frames arrive in order: advance() is
+// told how many leading frames of d_in are present and launches every step
+// for the frames whose windows those cover (maxima as frames arrive; moving
+// means avg_reach frames behind; eccentricity, threshold and smoothing a
+// further range_reach behind).  Once all P frames have arrived the result
+// equals launch_adaptive_filter's.  filtered() frames of d_out are final.
+struct AfStream {
+    explicit AfStream(const struct recon_metadata &mr);
+    int advance(const struct recon_metadata &mr, const float *d_in, float *d_out, float *d_scratch, int arrived,
+                cudaStream_t stream);
+    int filtered() const { return n_filtered; }
+    int P = 0, avg_reach = 0, range_reach = 0;
+    int n_sup = 0, n_smoothed = 0, n_filtered = 0;
+};
+
 }  // namespace ctbb

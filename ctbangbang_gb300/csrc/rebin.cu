@@ -225,6 +225,7 @@ struct RebinParams {
     const FocalTerm *focal;     // mode dependent
     float focal_offset[4];
     int n_ffs, N, Nos, R_raw, R, n_proj, add, n_views, reverse_rows;
+    int v_begin, v_end;  // views this launch writes
 };
 
 // View-axis coordinate of focal spot q at view proj, divided down to the index
@@ -264,7 +265,7 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int row = blockIdx.y;
-    int v0 = blockIdx.z * kViewsPerThread;
+    int v0 = p.v_begin + blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
     const Idx frame_stride = (Idx)p.R_raw * p.N;
     const Idx nos = (Idx)p.Nos;
@@ -278,7 +279,7 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
         const float *base = p.raw + (Idx)row * p.N + s * frame_stride;
         float *out = p.out + (Idx)out_row * nos + c;
 #pragma unroll 4
-        for (int v = v0; v < min(v0 + kViewsPerThread, p.n_views); ++v) {
+        for (int v = v0; v < min(v0 + kViewsPerThread, p.v_end); ++v) {
             float alpha = focal_alpha(p.n_ffs, v + p.add, t_alpha, t_off, s);
             int i0, i1;
             float w;
@@ -306,7 +307,7 @@ __global__ void rebin_two_stage_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int row = blockIdx.y;
-    int v0 = blockIdx.z * kViewsPerThread;
+    int v0 = p.v_begin + blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
     const Idx frame_stride = (Idx)p.R_raw * p.N;
     const Idx nos = (Idx)p.Nos;
@@ -324,7 +325,7 @@ __global__ void rebin_two_stage_kernel(RebinParams p)
         if (p.n_ffs == 4) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
         float *out = p.out + (Idx)out_row * nos + c;
 #pragma unroll 4
-        for (int v = v0; v < min(v0 + kViewsPerThread, p.n_views); ++v) {
+        for (int v = v0; v < min(v0 + kViewsPerThread, p.v_end); ++v) {
             int proj = v + p.add;
             int i0, i1;
             float w0, w1;
@@ -339,9 +340,21 @@ __global__ void rebin_two_stage_kernel(RebinParams p)
     }
 }
 
-int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float *d_raw,
-                 float *d_out, cudaStream_t stream)
+int rebin_frames_needed(const RebinTables &t, int v)
 {
+    // view-axis coordinate of a focal spot's frame sequence: proj - t_alpha /
+    // n_ffs - small focal terms, with |t_alpha| / n_ffs below the fan half
+    // angle in views, which add_projections exceeds by 10; +1 for the upper
+    // tap and one view of margin
+    return t.n_ffs * (v + 2 * t.add_projections + 2);
+}
+
+int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float *d_raw,
+                 float *d_out, cudaStream_t stream, int v_begin, int v_end)
+{
+    if (v_end < 0 || v_end > t.n_views) v_end = t.n_views;
+    if (v_begin < 0) v_begin = 0;
+    if (v_end <= v_begin) return CTBB_OK;
     RebinParams p;
     p.raw = d_raw;
     p.out = d_out;
@@ -357,7 +370,9 @@ int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float 
     p.add = t.add_projections;
     p.n_views = t.n_views;
     p.reverse_rows = t.reverse_rows;
-    int chunks = (t.n_views + kViewsPerThread - 1) / kViewsPerThread;
+    p.v_begin = v_begin;
+    p.v_end = v_end;
+    int chunks = (v_end - v_begin + kViewsPerThread - 1) / kViewsPerThread;
     if (chunks > 65535 || t.n_rows_raw > 65535) {
         set_error("rebin: %d views / %d rows exceed the launch grid", t.n_views, t.n_rows_raw);
         return CTBB_ERR_ARGUMENT;

@@ -40,7 +40,11 @@ struct DeviceRebinTables {
 
 int build_rebin_tables(const struct recon_metadata &mr, RebinTables *t);
 int upload_rebin_tables(const RebinTables &t, DeviceRebinTables *dt, cudaStream_t stream);
+// Views [v_begin, v_end) of the output (v_end < 0: all views).
 int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float *d_raw,
-                 float *d_out, cudaStream_t stream);
+                 float *d_out, cudaStream_t stream, int v_begin = 0, int v_end = -1);
+// Frames of the pull window view v reads (focal-spot frames of the view-axis
+// taps of every channel): all lie below rebin_frames_needed(t, v).
+int rebin_frames_needed(const RebinTables &t, int v);
 
 }  // namespace ctbb

@@ -352,6 +352,16 @@ int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
 int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan,
                                  float *d_final, float mu_water);
 
+/* ctbb_reconstruct_scan_device from host buffers, streamed (no counterpart in
+   the reference): the union window is copied host->device in chunks on a
+   second stream while each arriving chunk advances the adaptive filter as far
+   as its statistics windows allow, views whose frames are final are rebinned
+   and ramp-filtered, and each block is backprojected as soon as its views are
+   ready.  Same result as ctbb_reconstruct_scan_device.  Pin h_scan
+   (cudaHostRegister / cudaMallocHost) for the copies to overlap. */
+int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan,
+                               float *h_final, float mu_water);
+
 /* As ctbb_reconstruct_device from host buffers: each block's pull window is
    copied from h_scan [n_readings][n_rows_raw][n_channels] on a second stream
    (double-buffered, overlapping the previous block's compute when h_scan is

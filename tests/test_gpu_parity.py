@@ -346,3 +346,31 @@ def test_whole_scan_path_vs_block_loop(torch_cuda, lib, tmp_path, strength):
     else:
         assert mx <= HU_MAX and rms <= HU_RMS, (mx, rms)
     scan.close()
+
+
+def test_whole_scan_streamed_from_host_equals_device_path(torch_cuda, lib, tmp_path):
+    """The streamed host path runs the same kernels on the same data as the
+    device whole-scan path, only scheduled as the chunks arrive: bit-exact.
+    Another scan runs first so that no work buffer holds this scan's data."""
+    torch = torch_cuda
+    other = H.Scan(scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=44),
+                   str(tmp_path / "other"))
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=45)
+    scan = H.Scan(spec, str(tmp_path / "scan"))
+    mr = scan.mr
+    assert mr.ri.n_blocks >= 2
+    n_final = lib.ctbb_n_slices_final(C.byref(mr))
+    plane = mr.rp.nx * mr.rp.ny
+    d_other = dev(torch, other.frames.reshape(-1))
+    d_junk = torch.empty(lib.ctbb_n_slices_final(C.byref(other.mr)) * plane, dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_scan_device", C.byref(other.mr), ptr(d_other), ptr(d_junk), 0.0)
+    torch.cuda.synchronize()
+    h_scan = np.ascontiguousarray(scan.frames.reshape(-1), dtype=np.float32)
+    h_final = np.zeros(n_final * plane, np.float32)
+    L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(h_scan), fptr(h_final), 0.0)
+    d_scan = dev(torch, h_scan)
+    d_fin = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_scan_device", C.byref(mr), ptr(d_scan), ptr(d_fin), 0.0)
+    np.testing.assert_array_equal(h_final, d_fin.cpu().numpy())
+    other.close()
+    scan.close()
