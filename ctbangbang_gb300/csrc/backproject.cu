@@ -57,6 +57,8 @@ struct BpParams {
     float zrot_over_2pi;
     float tan_cone;
     int k_window;          // half-turn window per angle (z_rot != 0)
+    int warp_w;            // voxel columns along x per warp (32, 16, 8 or 4)
+    int cta_w;             // voxel columns along x per CTA (a multiple of warp_w)
     float abs_zr;          // |z_rot / (2 pi')|
     float inv_half_feed;   // 2 / z_rot: half turns per mm of ray travel
     float half_rows;       // (R - 1) / 2
@@ -139,8 +141,13 @@ template <int ZPT, int MIN_BLOCKS, int NOS>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
     const int nos = NOS > 0 ? NOS : p.nos;
-    int xi = blockIdx.x * blockDim.x + threadIdx.x;
-    int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    // A CTA covers cta_w x (256 / cta_w) voxel columns; each warp a warp_w x
+    // (32 / warp_w) sub-tile, which bounds how far apart its lanes' detector
+    // samples lie (a row of 32 columns spreads over up to ~110 channels).
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tiles_x = p.cta_w / p.warp_w;
+    int xi = blockIdx.x * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
+    int yi = blockIdx.y * (256 / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
     int z0 = blockIdx.z * ZPT;
     if (xi >= p.nx || yi >= p.ny) return;
     // voxel centre with the reference's float operations (no contraction)
@@ -360,6 +367,30 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
         if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z * 256] * p.out_scale;
 }
 
+// Voxel columns along x per CTA of the backprojector (256 columns per CTA).
+// Measured on config 2 (ms per 32-slice block): warps of 32 x 1 columns 21.9,
+// 16 x 2 20.4, 8 x 4 19.4-19.8, 4 x 8 19.5-19.7; CTAs of 64 x 4 best by 1 %.
+int bp_cta_width()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_CTA_W");
+        int w = e ? atoi(e) : 64;
+        return (w == 8 || w == 16 || w == 32 || w == 64 || w == 128) ? w : 32;
+    }();
+    return v;
+}
+
+// Voxel columns along x per warp of the backprojector's CTA tile.
+int bp_warp_width()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_WARP_W");
+        int w = e ? atoi(e) : 8;
+        return (w == 4 || w == 8 || w == 16 || w == 32) ? w : 32;
+    }();
+    return v;
+}
+
 // CTAs per SM the backprojector is compiled for (3: 80 registers, 4: 64)
 int bp_min_blocks()
 {
@@ -454,36 +485,31 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
         set_error("backproject: detector too small");
         return CTBB_ERR_ARGUMENT;
     }
+    p.warp_w = bp_warp_width();
+    p.cta_w = std::max(bp_cta_width(), p.warp_w);
+    if (256 / p.cta_w < 32 / p.warp_w) p.cta_w = 8 * p.warp_w;  // whole warp tiles in y
     dim3 block(32, 8);
-    dim3 grid((p.nx + 31) / 32, (p.ny + 7) / 8, 1);
+    dim3 grid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + 256 / p.cta_w - 1) / (256 / p.cta_w), 1);
     auto go = [&](auto zpt_tag) {
         constexpr int Z = decltype(zpt_tag)::value;
         grid.z = (p.n_slices + Z - 1) / Z;
-        constexpr int MB = Z <= 8 ? 3 : 2;
+        // 8 slices: 4 CTAs per SM by default (64 registers), 3 on request;
+        // 16 slices: 3 CTAs (80 registers); the row lengths of the built-in
+        // scanners with flying focal spot get a compile-time row stride
+        auto launch = [&](auto mb_tag) {
+            constexpr int MB = decltype(mb_tag)::value;
+            if (p.nos == 1472) backproject_kernel<Z, MB, 1472><<<grid, block, 0, stream>>>(p);
+            else if (p.nos == 1344) backproject_kernel<Z, MB, 1344><<<grid, block, 0, stream>>>(p);
+            else backproject_kernel<Z, MB, 0><<<grid, block, 0, stream>>>(p);
+        };
         if constexpr (Z == 8) {
-            // the row lengths of the built-in scanners with flying focal spot
-            if (bp_min_blocks() == 4) {
-                if (p.nos == 1472) {
-                    backproject_kernel<8, 4, 1472><<<grid, block, 0, stream>>>(p);
-                    return;
-                }
-                if (p.nos == 1344) {
-                    backproject_kernel<8, 4, 1344><<<grid, block, 0, stream>>>(p);
-                    return;
-                }
-                backproject_kernel<8, 4, 0><<<grid, block, 0, stream>>>(p);
-                return;
-            }
-            if (p.nos == 1472) {
-                backproject_kernel<8, MB, 1472><<<grid, block, 0, stream>>>(p);
-                return;
-            }
-            if (p.nos == 1344) {
-                backproject_kernel<8, MB, 1344><<<grid, block, 0, stream>>>(p);
-                return;
-            }
+            if (bp_min_blocks() == 4) launch(std::integral_constant<int, 4>());
+            else launch(std::integral_constant<int, 3>());
+        } else if constexpr (Z == 16) {
+            launch(std::integral_constant<int, 3>());
+        } else {
+            backproject_kernel<Z, 3, 0><<<grid, block, 0, stream>>>(p);
         }
-        backproject_kernel<Z, MB, 0><<<grid, block, 0, stream>>>(p);
     };
     switch (zpt) {
     case 16: go(std::integral_constant<int, 16>()); break;
