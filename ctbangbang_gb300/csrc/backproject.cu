@@ -68,6 +68,8 @@ struct BpParams {
 };
 
 constexpr float kQ = 0.6f;
+// slices per sub-chunk: the unit of the flat / inner / other decision
+constexpr int kSub = 8;
 
 // interp2 drops a sample when q_idx > R*nht - 2, which only the last half
 // turn can reach.  Its weight still counts, so the decision is a jump in the
@@ -140,6 +142,7 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 template <int ZPT, int MIN_BLOCKS, int NOS>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
+    constexpr int SUB = ZPT < kSub ? ZPT : kSub;  // slices per sub-chunk
     const int nos = NOS > 0 ? NOS : p.nos;
     // A CTA covers cta_w x (256 / cta_w) voxel columns; each warp a warp_w x
     // (32 / warp_w) sub-tile, which bounds how far apart its lanes' detector
@@ -174,7 +177,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
 
     for (int i = 0; i < p.n_half; ++i) {
         float2 s2[ZPT / 2], h2[ZPT / 2];  // per-angle sums of slice pairs
-        int n_flat = 0;  // flat visits of this angle: W = 1 for every slice
+        int n_flat[ZPT / SUB];  // flat visits of each sub-chunk: W = 1 for every slice
+#pragma unroll
+        for (int sc = 0; sc < ZPT / SUB; ++sc) n_flat[sc] = 0;
 #pragma unroll
         for (int m = 0; m < ZPT / 2; ++m) {
             s2[m] = make_float2(0.0f, 0.0f);
@@ -232,15 +237,6 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
             const float *view = p.rebin + (size_t)(i + k * p.n_half) * view_stride + ip;
-            // Chunk classes, decided per warp so that no two paths both run
-            // (q is monotone in z, so |q| is largest at an end of the chunk):
-            //  flat:  every |q| <= Q, so W = 1; with R >= 8 every row lies in
-            //         [0, R-2] and below the last-turn border;
-            //  inner: every |q| < 1, so every row lies in [0, R-2]; in the last
-            //         half turn also every row well below its border;
-            //  other: per-slice validity, clamped rows, last-turn border.
-            float a_max = fmaxf(fabsf(q0), fabsf(q_end));
-            unsigned lanes = __activemask();
             // Slices are processed in pairs (z, z + 1) with packed FP32
             // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
             // conversions and loads stay per slice.
@@ -266,52 +262,102 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                 float2 c = make_float2(__cosf(arg.x), __cosf(arg.y));
                 return mul2(c, c);
             };
-            if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
-                if (p_ok) {
-                    float ql0 = fmaf(q0, p.half_rows, p.half_rows);
-                    float dql = dq * p.half_rows;
-                    const float2 ql02 = make_float2(ql0, ql0), dql2 = make_float2(dql, dql);
+            // Sub-chunks of SUB slices share the geometry above.  Each is
+            // skipped when no lane has a slice inside |q| < 1, else classed per
+            // warp so that no two paths both run
+            // (q is monotone in z, so |q| is largest at an end of the chunk):
+            //  flat:  every |q| <= Q, so W = 1; with R >= 8 every row lies in
+            //         [0, R-2] and below the last-turn border;
+            //  inner: every |q| < 1, so every row lies in [0, R-2]; in the last
+            //         half turn also every row well below its border;
+            //  other: per-slice validity, clamped rows, last-turn border.
+            unsigned lanes = __activemask();
 #pragma unroll
-                    for (int m = 0; m < ZPT / 2; ++m) {
-                        float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
-                        float2 row = make_float2(floorf(ql.x), floorf(ql.y));
-                        s2[m] = add2(s2[m], pair_value(ql, row));
+            for (int sc = 0; sc < ZPT / SUB; ++sc) {
+                const float q0c = fmaf((float)(sc * SUB), dq, q0);
+                const float q_endc = fmaf((float)(sc * SUB + SUB - 1), dq, q0);
+                if (ZPT > SUB && __all_sync(lanes, q0c >= 1.0f || q_endc <= -1.0f)) continue;
+                float a_max = fmaxf(fabsf(q0c), fabsf(q_endc));
+                if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
+                    if (p_ok) {
+                        float ql0 = fmaf(q0, p.half_rows, p.half_rows);
+                        float dql = dq * p.half_rows;
+                        const float2 ql02 = make_float2(ql0, ql0), dql2 = make_float2(dql, dql);
+#pragma unroll
+                        for (int mm = 0; mm < SUB / 2; ++mm) {
+                            const int m = sc * (SUB / 2) + mm;
+                            float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
+                            float2 row = make_float2(floorf(ql.x), floorf(ql.y));
+                            s2[m] = add2(s2[m], pair_value(ql, row));
+                        }
                     }
+                    ++n_flat[sc];
+                    continue;
                 }
-                ++n_flat;
-                continue;
-            }
-            bool inner = a_max < kInnerMax && (!last || fmaf(a_max, p.half_rows, p.half_rows) < q_max_last - kRowMargin);
-            if (__all_sync(lanes, inner)) {
-                if (p_ok) {
+                bool inner = a_max < kInnerMax && (!last || fmaf(a_max, p.half_rows, p.half_rows) < q_max_last - kRowMargin);
+                if (__all_sync(lanes, inner)) {
+                    if (p_ok) {
 #pragma unroll
-                    for (int m = 0; m < ZPT / 2; ++m) {
+                        for (int mm = 0; mm < SUB / 2; ++mm) {
+                            const int m = sc * (SUB / 2) + mm;
+                            float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                            float2 w = pair_weight(q);
+                            h2[m] = add2(h2[m], w);
+                            float2 ql = fma2(q, hr2, hr2);
+                            float2 row = make_float2(floorf(ql.x), floorf(ql.y));
+                            s2[m] = fma2(w, pair_value(ql, row), s2[m]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int mm = 0; mm < SUB / 2; ++mm) {
+                            const int m = sc * (SUB / 2) + mm;
+                            float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                            h2[m] = add2(h2[m], pair_weight(q));
+                        }
+                    }
+                    continue;
+                }
+                // Other chunks.  Branch-free gathers: every slice loads its 2x2
+                // footprint from inside the view (row clamped to [0, R-2], channel 0
+                // when p is off the detector) and validity only scales the weight, so
+                // the loads of all slices can be issued together.  Only a warp with
+                // a row near the last-turn border takes the per-slice border test.
+                const float row_max = (float)(p.n_rows - 2);
+                bool border = last && fmaf(q_endc, p.half_rows, p.half_rows) > q_max_last - kBorderBand;
+                if (__any_sync(lanes, border)) {
+#pragma unroll
+                    for (int mm = 0; mm < SUB / 2; ++mm) {
+                        const int m = sc * (SUB / 2) + mm;
                         float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                         float2 w = pair_weight(q);
+                        w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
                         h2[m] = add2(h2[m], w);
                         float2 ql = fma2(q, hr2, hr2);
-                        float2 row = make_float2(floorf(ql.x), floorf(ql.y));
-                        s2[m] = fma2(w, pair_value(ql, row), s2[m]);
+                        float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
+                                                 fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
+                        float2 v = pair_value(ql, row);
+                        bool ok_x = p_ok && in_x, ok_y = p_ok && in_y;
+                        if (ok_x) {
+                            float d = ql.x - q_max_last;
+                            if (d > kBorderBand) ok_x = false;
+                            else if (d > -kBorderBand)
+                                ok_x = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + 2 * m), k);
+                        }
+                        if (ok_y) {
+                            float d = ql.y - q_max_last;
+                            if (d > kBorderBand) ok_y = false;
+                            else if (d > -kBorderBand)
+                                ok_y = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat,
+                                                              __ldg(p.zpos + z0 + 2 * m + 1), k);
+                        }
+                        s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
                     }
-                } else {
-#pragma unroll
-                    for (int m = 0; m < ZPT / 2; ++m) {
-                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
-                        h2[m] = add2(h2[m], pair_weight(q));
-                    }
+                    continue;
                 }
-                continue;
-            }
-            // Other chunks.  Branch-free gathers: every slice loads its 2x2
-            // footprint from inside the view (row clamped to [0, R-2], channel 0
-            // when p is off the detector) and validity only scales the weight, so
-            // the loads of all slices can be issued together.  Only a warp with
-            // a row near the last-turn border takes the per-slice border test.
-            const float row_max = (float)(p.n_rows - 2);
-            bool border = last && fmaf(q_end, p.half_rows, p.half_rows) > q_max_last - kBorderBand;
-            if (__any_sync(lanes, border)) {
 #pragma unroll
-                for (int m = 0; m < ZPT / 2; ++m) {
+                for (int mm = 0; mm < SUB / 2; ++mm) {
+                    const int m = sc * (SUB / 2) + mm;
                     float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
                     bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                     float2 w = pair_weight(q);
@@ -321,41 +367,14 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                     float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
                                              fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
                     float2 v = pair_value(ql, row);
-                    bool ok_x = p_ok && in_x, ok_y = p_ok && in_y;
-                    if (ok_x) {
-                        float d = ql.x - q_max_last;
-                        if (d > kBorderBand) ok_x = false;
-                        else if (d > -kBorderBand)
-                            ok_x = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + 2 * m), k);
-                    }
-                    if (ok_y) {
-                        float d = ql.y - q_max_last;
-                        if (d > kBorderBand) ok_y = false;
-                        else if (d > -kBorderBand)
-                            ok_y = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat,
-                                                          __ldg(p.zpos + z0 + 2 * m + 1), k);
-                    }
-                    s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
+                    s2[m] = fma2(p_ok ? w : make_float2(0.0f, 0.0f), v, s2[m]);
                 }
-                continue;
-            }
-#pragma unroll
-            for (int m = 0; m < ZPT / 2; ++m) {
-                float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
-                bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
-                float2 w = pair_weight(q);
-                w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
-                h2[m] = add2(h2[m], w);
-                float2 ql = fma2(q, hr2, hr2);
-                float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
-                                         fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
-                float2 v = pair_value(ql, row);
-                s2[m] = fma2(p_ok ? w : make_float2(0.0f, 0.0f), v, s2[m]);
             }
         }
 #pragma unroll
         for (int m = 0; m < ZPT / 2; ++m) {
-            float2 hz = add2(h2[m], make_float2((float)n_flat, (float)n_flat));
+            const float nf = (float)n_flat[m / (SUB / 2)];
+            float2 hz = add2(h2[m], make_float2(nf, nf));
             float rx = __fdividef(s2[m].x, hz.x), ry = __fdividef(s2[m].y, hz.y);
             img[(2 * m) * 256] += hz.x != 0.0f ? rx : 0.0f;
             img[(2 * m + 1) * 256] += hz.y != 0.0f ? ry : 0.0f;
@@ -506,7 +525,8 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
             if (bp_min_blocks() == 4) launch(std::integral_constant<int, 4>());
             else launch(std::integral_constant<int, 3>());
         } else if constexpr (Z == 16) {
-            launch(std::integral_constant<int, 3>());
+            if (bp_min_blocks() == 2) launch(std::integral_constant<int, 2>());
+            else launch(std::integral_constant<int, 3>());
         } else {
             backproject_kernel<Z, 3, 0><<<grid, block, 0, stream>>>(p);
         }
