@@ -159,11 +159,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
 
     // the image sums live in shared memory (touched once per angle), which
     // leaves the registers to the per-angle sums and the gathers in flight
-    __shared__ float img_sh[ZPT][256];
+    __shared__ float2 img_sh[ZPT / 2][256];  // slice pairs, one 8-byte word per thread
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    float *img = &img_sh[0][tid];
+    float2 *img = &img_sh[0][tid];
 #pragma unroll
-    for (int z = 0; z < ZPT; ++z) img[z * 256] = 0.0f;
+    for (int m = 0; m < ZPT / 2; ++m) img[m * 256] = make_float2(0.0f, 0.0f);
     // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
     // is only needed by the border recheck and is read from zpos there)
     const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
@@ -375,15 +375,20 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
         for (int m = 0; m < ZPT / 2; ++m) {
             const float nf = (float)n_flat[m / (SUB / 2)];
             float2 hz = add2(h2[m], make_float2(nf, nf));
-            float rx = __fdividef(s2[m].x, hz.x), ry = __fdividef(s2[m].y, hz.y);
-            img[(2 * m) * 256] += hz.x != 0.0f ? rx : 0.0f;
-            img[(2 * m + 1) * 256] += hz.y != 0.0f ? ry : 0.0f;
+            // s is 0 wherever h is (every weight that adds to s adds to h), and
+            // the smallest nonzero h is far above 1e-30: s / max(h, 1e-30) is
+            // the reference's "if (h != 0) img += s / h"
+            float2 rh = make_float2(__fdividef(1.0f, fmaxf(hz.x, 1e-30f)), __fdividef(1.0f, fmaxf(hz.y, 1e-30f)));
+            img[m * 256] = fma2(s2[m], rh, img[m * 256]);
         }
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
     for (int z = 0; z < ZPT; ++z)
-        if (z0 + z < p.n_slices) p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = img[z * 256] * p.out_scale;
+        if (z0 + z < p.n_slices) {
+            float2 v = img[(z / 2) * 256];
+            p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = ((z & 1) ? v.y : v.x) * p.out_scale;
+        }
 }
 
 // Voxel columns along x per CTA of the backprojector (256 columns per CTA).
