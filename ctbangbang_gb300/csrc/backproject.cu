@@ -44,7 +44,7 @@ namespace {
 struct BpParams {
     const float *rebin;    // [V][R][Nos]
     float *out;            // [n_slices_block][ny][nx]
-    const float4 *views;   // [n_half][nht] {theta, sin, cos, 0}
+    const float4 *views;   // [n_half][nht] {theta, sin, cos, theta z_rot / 2 pi'}
     const float *zpos;     // [n_slices_block]
     int nx, ny, n_slices, nos, n_rows, nht, n_half;
     float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
     // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
     // is only needed by the border recheck and is read from zpos there)
     const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
-    const size_t view_stride = (size_t)p.n_rows * nos;
+    const unsigned view_stride = (unsigned)(p.n_rows * nos);  // < 2^20
     const float p_max = (float)(nos - 2);
     const float p_mid = 0.5f * p_max;
     const float q_max_last = (float)(p.n_rows - 2);
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                 // angles and of this bound; the exact test below still decides
                 // every visited half turn.
                 float reach = fmaf(root + fabsf(fmaf(x, t0.z, y * t0.y)), p.tan_cone, a_abs * p.abs_zr);
-                float base = t0.x * p.zrot_over_2pi;
+                float base = t0.w;
                 float lo = (z_lo - reach - base) * p.inv_half_feed;
                 float hi = (z_hi + reach - base) * p.inv_half_feed;
                 k_lo = max(k_lo, (int)ceilf(fminf(lo, hi) - kWindowMargin));
@@ -218,10 +218,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             float4 t = __ldg(vt + k);
             // q of the chunk's slices: q(z) = q0 + z dq (dq > 0)
             float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
-            float ray = (t.x - copysignf(a_abs, phat)) * p.zrot_over_2pi;
+            // zbase - ray with ray = (theta - asin(p / r_f)) z_rot / 2 pi'
+            float zb_ray = fmaf(copysignf(a_abs, phat), p.zrot_over_2pi, zbase - t.w);
             float lhat = root - x * t.z - y * t.y;
             float inv_den = __fdividef(1.0f, lhat * p.tan_cone);
-            float q0 = (zbase - ray) * inv_den;
+            float q0 = zb_ray * inv_den;
             float dq = p.coll * inv_den;
             float q_end = fmaf((float)(ZPT - 1), dq, q0);
             // no slice of the chunk inside |q| < 1: nothing to add, not even weight
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
-            const float *view = p.rebin + (size_t)(i + k * p.n_half) * view_stride + ip;
+            const float *view = p.rebin + (size_t)(unsigned)(i + k * p.n_half) * view_stride + ip;
             // Slices are processed in pairs (z, z + 1) with packed FP32
             // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
             // conversions and loads stay per slice.
@@ -450,7 +451,7 @@ int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables 
             v[0] = theta;
             v[1] = std::sin(theta);
             v[2] = std::cos(theta);
-            v[3] = 0.0f;
+            v[3] = theta * (cg.z_rot / (2.0f * pi));  // theta z_rot / 2 pi': the ray's table term
         }
     t->zpos.resize(t->n_slices);
     for (int zi = 0; zi < t->n_slices; ++zi)  // src/backproject_cpu.cu:107

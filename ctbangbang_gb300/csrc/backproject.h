@@ -14,7 +14,7 @@ struct BackprojectTables {
     int nht = 0;               // half turns in the pull window
     int n_half = 0;            // n_proj_turn / 2
     int n_slices = 0;          // slices per block
-    std::vector<float> views;  // [n_half][nht][4] {theta, sin, cos, 0}
+    std::vector<float> views;  // [n_half][nht][4] {theta, sin, cos, theta z_rot / 2 pi'}
     std::vector<float> zpos;   // [n_slices]
 };
 
