@@ -361,6 +361,8 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
                     const int m = sc * (SUB / 2) + mm;
                     float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
                     bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
+                    // a pair outside |q| < 1 in every lane adds nothing
+                    if (!__any_sync(lanes, in_x || in_y)) continue;
                     float2 w = pair_weight(q);
                     w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
                     h2[m] = add2(h2[m], w);
