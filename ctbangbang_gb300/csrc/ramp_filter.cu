@@ -240,16 +240,21 @@ __device__ __forceinline__ float2 mul_omega4(float2 z)
     return SIGN < 0 ? make_float2(z.y, -z.x) : make_float2(-z.y, z.x);
 }
 
+// Complex add / subtract as packed FP32 pairs (sm_100 family: one
+// instruction for the real and imaginary parts).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+
 // In-place 4-point DFT of (a, b, c, d), outputs in natural order.
 template <int SIGN>
 __device__ __forceinline__ void dft4(float2 &a, float2 &b, float2 &c, float2 &d)
 {
-    float2 s0 = make_float2(a.x + c.x, a.y + c.y), d0 = make_float2(a.x - c.x, a.y - c.y);
-    float2 s1 = make_float2(b.x + d.x, b.y + d.y), d1 = mul_omega4<SIGN>(make_float2(b.x - d.x, b.y - d.y));
-    a = make_float2(s0.x + s1.x, s0.y + s1.y);
-    c = make_float2(s0.x - s1.x, s0.y - s1.y);
-    b = make_float2(d0.x + d1.x, d0.y + d1.y);
-    d = make_float2(d0.x - d1.x, d0.y - d1.y);
+    float2 s0 = cadd(a, c), d0 = csub(a, c);
+    float2 s1 = cadd(b, d), d1 = mul_omega4<SIGN>(csub(b, d));
+    a = cadd(s0, s1);
+    c = csub(s0, s1);
+    b = cadd(d0, d1);
+    d = csub(d0, d1);
 }
 
 // z * exp(SIGN 2 pi i e / 16) for the internal twiddles of the 4 x 4 split
@@ -279,10 +284,10 @@ __device__ __forceinline__ void dft16(float2 (&v)[16])
         if (HALF) {
             float2 a = v[n2], b = v[n2 + 4];
             float2 wb = mul_omega4<SIGN>(b);
-            v[n2] = make_float2(a.x + b.x, a.y + b.y);
-            v[n2 + 4] = make_float2(a.x + wb.x, a.y + wb.y);
-            v[n2 + 8] = make_float2(a.x - b.x, a.y - b.y);
-            v[n2 + 12] = make_float2(a.x - wb.x, a.y - wb.y);
+            v[n2] = cadd(a, b);
+            v[n2 + 4] = cadd(a, wb);
+            v[n2 + 8] = csub(a, b);
+            v[n2 + 12] = csub(a, wb);
         } else {
             dft4<SIGN>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
         }
