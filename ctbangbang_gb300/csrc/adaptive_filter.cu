@@ -250,29 +250,56 @@ __device__ __noinline__ float smooth_sample(const AfParams &p, int gp, int gr, i
 }
 
 // Streaming form for rows of a multiple of 4 channels: one CTA per frame
-// copies the frame with float4 loads/stores and smooths only the samples above
-// the frame's threshold -- about 1e-4 of them on clinical-size scans -- so the
-// kernel runs at copy speed.  Same arithmetic, same result as the tiled form.
+// copies the frame with float4 loads/stores and notes the samples above the
+// frame's threshold -- about 1e-4 of them on clinical-size scans -- in a
+// shared-memory list; after the copy the CTA smooths the listed samples (or,
+// when the list overflowed, every sample above the threshold again).  The
+// copy loop holds no call, so it runs at copy speed.  Same arithmetic, same
+// result as the tiled form.
+constexpr int kSmoothListMax = 1024;
+
 __global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
 {
+    __shared__ int list[kSmoothListMax];
+    __shared__ int n_list;
     int gp = p.f0 + blockIdx.x;
     size_t frame = (size_t)p.R * p.N;
     const float4 *src = reinterpret_cast<const float4 *>(p.raw + (size_t)gp * frame);
     float4 *dst = reinterpret_cast<float4 *>(p.out + (size_t)gp * frame);
+    float *dst1 = p.out + (size_t)gp * frame;
     const float T = __ldg(p.thr + gp);
     const int n4 = (int)(frame / 4);
-    const int row4 = p.N / 4;
+    if (threadIdx.x == 0) n_list = 0;
+    __syncthreads();
     for (int i = threadIdx.x; i < n4; i += blockDim.x) {
         float4 v = __ldg(src + i);
-        if (v.x > T || v.y > T || v.z > T || v.w > T) {
-            int gr = i / row4;
-            int gc = (i - gr * row4) * 4;
-            if (v.x > T) v.x = smooth_sample(p, gp, gr, gc);
-            if (v.y > T) v.y = smooth_sample(p, gp, gr, gc + 1);
-            if (v.z > T) v.z = smooth_sample(p, gp, gr, gc + 2);
-            if (v.w > T) v.w = smooth_sample(p, gp, gr, gc + 3);
-        }
         dst[i] = v;
+        if (v.x > T || v.y > T || v.z > T || v.w > T) {
+            float c[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (c[e] > T) {
+                    int slot = atomicAdd(&n_list, 1);
+                    if (slot < kSmoothListMax) list[slot] = 4 * i + e;
+                }
+        }
+    }
+    __syncthreads();
+    const int n = n_list;
+    if (n <= kSmoothListMax) {
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            int e = list[j];
+            int gr = e / p.N, gc = e - gr * p.N;
+            dst1[e] = smooth_sample(p, gp, gr, gc);
+        }
+    } else {
+        const float *src1 = p.raw + (size_t)gp * frame;
+        for (int e = threadIdx.x; e < (int)frame; e += blockDim.x) {
+            if (__ldg(src1 + e) > T) {
+                int gr = e / p.N, gc = e - gr * p.N;
+                dst1[e] = smooth_sample(p, gp, gr, gc);
+            }
+        }
     }
 }
 
