@@ -139,8 +139,8 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 
 // NOS > 0: the row length as a compile-time constant (the second row of a
 // footprint is then an immediate offset); 0: taken from p.nos.
-template <int ZPT, int MIN_BLOCKS, int NOS>
-__global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p)
+template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS = 256>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
     constexpr int SUB = ZPT < kSub ? ZPT : kSub;  // slices per sub-chunk
     const int nos = NOS > 0 ? NOS : p.nos;
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tiles_x = p.cta_w / p.warp_w;
     int xi = blockIdx.x * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
-    int yi = blockIdx.y * (256 / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
+    int yi = blockIdx.y * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
     int z0 = blockIdx.z * ZPT;
     if (xi >= p.nx || yi >= p.ny) return;
     // voxel centre with the reference's float operations (no contraction)
@@ -159,11 +159,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
 
     // the image sums live in shared memory (touched once per angle), which
     // leaves the registers to the per-angle sums and the gathers in flight
-    __shared__ float2 img_sh[ZPT / 2][256];  // slice pairs, one 8-byte word per thread
+    __shared__ float2 img_sh[ZPT / 2][THREADS];  // slice pairs, one 8-byte word per thread
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     float2 *img = &img_sh[0][tid];
 #pragma unroll
-    for (int m = 0; m < ZPT / 2; ++m) img[m * 256] = make_float2(0.0f, 0.0f);
+    for (int m = 0; m < ZPT / 2; ++m) img[m * THREADS] = make_float2(0.0f, 0.0f);
     // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
     // is only needed by the border recheck and is read from zpos there)
     const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
@@ -382,16 +382,27 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) backproject_kernel(BpParams p
             // the smallest nonzero h is far above 1e-30: s / max(h, 1e-30) is
             // the reference's "if (h != 0) img += s / h"
             float2 rh = make_float2(__fdividef(1.0f, fmaxf(hz.x, 1e-30f)), __fdividef(1.0f, fmaxf(hz.y, 1e-30f)));
-            img[m * 256] = fma2(s2[m], rh, img[m * 256]);
+            img[m * THREADS] = fma2(s2[m], rh, img[m * THREADS]);
         }
     }
     size_t plane = (size_t)p.nx * p.ny;
 #pragma unroll
     for (int z = 0; z < ZPT; ++z)
         if (z0 + z < p.n_slices) {
-            float2 v = img[(z / 2) * 256];
+            float2 v = img[(z / 2) * THREADS];
             p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = ((z & 1) ? v.y : v.x) * p.out_scale;
         }
+}
+
+// Threads (voxel columns) per CTA of the backprojector: 256 or 128.
+int bp_cta_threads()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_THREADS");
+        int t = e ? atoi(e) : 128;
+        return t == 256 ? 256 : 128;
+    }();
+    return v;
 }
 
 // Voxel columns along x per CTA of the backprojector (256 columns per CTA).
@@ -418,12 +429,13 @@ int bp_warp_width()
     return v;
 }
 
-// CTAs per SM the backprojector is compiled for (3: 80 registers, 4: 64)
+// CTAs per SM the backprojector is compiled for: 128-thread CTAs 7 (72
+// registers, default) or 8 (64); 256-thread CTAs 4 (64) or 3 (80).
 int bp_min_blocks()
 {
     static int v = [] {
         const char *e = getenv("CTBB_BP_MINB");
-        return e ? atoi(e) : 4;
+        return e ? atoi(e) : 7;
     }();
     return v;
 }
@@ -512,29 +524,43 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
         set_error("backproject: detector too small");
         return CTBB_ERR_ARGUMENT;
     }
+    const int threads = zpt == 8 ? bp_cta_threads() : 256;
     p.warp_w = bp_warp_width();
     p.cta_w = std::max(bp_cta_width(), p.warp_w);
-    if (256 / p.cta_w < 32 / p.warp_w) p.cta_w = 8 * p.warp_w;  // whole warp tiles in y
-    dim3 block(32, 8);
-    dim3 grid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + 256 / p.cta_w - 1) / (256 / p.cta_w), 1);
+    if (threads / p.cta_w < 32 / p.warp_w) p.cta_w = (threads / 32) * p.warp_w;  // whole warp tiles in y
+    const int cta_h = threads / p.cta_w;
+    dim3 block(32, threads / 32);
+    dim3 grid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + cta_h - 1) / cta_h, 1);
     auto go = [&](auto zpt_tag) {
         constexpr int Z = decltype(zpt_tag)::value;
         grid.z = (p.n_slices + Z - 1) / Z;
         // 8 slices: 4 CTAs per SM by default (64 registers), 3 on request;
         // 16 slices: 3 CTAs (80 registers); the row lengths of the built-in
         // scanners with flying focal spot get a compile-time row stride
-        auto launch = [&](auto mb_tag) {
+        // the kernel for the row length in hand: compile-time strides only for
+        // the row lengths they were compiled for, the runtime stride otherwise
+        auto launch = [&](auto mb_tag, auto threads_tag) {
             constexpr int MB = decltype(mb_tag)::value;
-            if (p.nos == 1472) backproject_kernel<Z, MB, 1472><<<grid, block, 0, stream>>>(p);
-            else if (p.nos == 1344) backproject_kernel<Z, MB, 1344><<<grid, block, 0, stream>>>(p);
-            else backproject_kernel<Z, MB, 0><<<grid, block, 0, stream>>>(p);
+            constexpr int T = decltype(threads_tag)::value;
+            if (p.nos == 1472) backproject_kernel<Z, MB, 1472, T><<<grid, block, 0, stream>>>(p);
+            else if (p.nos == 1344) backproject_kernel<Z, MB, 1344, T><<<grid, block, 0, stream>>>(p);
+            else backproject_kernel<Z, MB, 0, T><<<grid, block, 0, stream>>>(p);
         };
+        using T128 = std::integral_constant<int, 128>;
+        using T256 = std::integral_constant<int, 256>;
         if constexpr (Z == 8) {
-            if (bp_min_blocks() == 4) launch(std::integral_constant<int, 4>());
-            else launch(std::integral_constant<int, 3>());
+            if (threads == 128) {
+                // 128-thread CTAs: 7 per SM (72 registers) by default, or 8 (64)
+                if (bp_min_blocks() == 8) launch(std::integral_constant<int, 8>(), T128());
+                else launch(std::integral_constant<int, 7>(), T128());
+            } else if (bp_min_blocks() == 3) {
+                launch(std::integral_constant<int, 3>(), T256());
+            } else {
+                launch(std::integral_constant<int, 4>(), T256());
+            }
         } else if constexpr (Z == 16) {
-            if (bp_min_blocks() == 2) launch(std::integral_constant<int, 2>());
-            else launch(std::integral_constant<int, 3>());
+            if (bp_min_blocks() == 2) launch(std::integral_constant<int, 2>(), T256());
+            else launch(std::integral_constant<int, 3>(), T256());
         } else {
             backproject_kernel<Z, 3, 0><<<grid, block, 0, stream>>>(p);
         }
