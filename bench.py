@@ -96,6 +96,17 @@ def block_plans(mr):
     return out
 
 
+def workload_text(name, spec, mr, n_blocks, n_final):
+    """One line naming the workload by its sizes."""
+    ffs = {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(spec.z_ffs, spec.phi_ffs)]
+    text = ("%s: %d ch x %d rows %s -> %d x %d, %d views/turn, pitch %.2g, %g turns, %d^2 x %d slices (%d blocks)"
+            % (name, mr.cg.n_channels, mr.cg.n_rows_raw, ffs, mr.cg.n_channels_oversampled, mr.cg.n_rows,
+               mr.cg.n_proj_turn, spec.pitch, spec.turns, mr.rp.nx, mr.ri.n_slices_recon, n_blocks))
+    if n_final is not None:
+        text += " thickened to %d x %g mm" % (n_final, spec.slice_thickness)
+    return text + ("; adaptive filter on" if spec.adaptive_filtration > 0 else "")
+
+
 def workload_sizes(mr, blocks):
     nht = [(ri.n_proj_pull // ri.n_ffs - 2 * mr.cg.add_projections) // (mr.cg.n_proj_turn // 2) for ri in blocks]
     plane = mr.rp.nx * mr.rp.ny
@@ -279,7 +290,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": cb["scan_seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded helical phantom (config-2 geometry)",
-        "config": {"workload": "%s: full-FFS helical wFBP, 3 blocks of 512^2 x 32" % args.config,
+        "config": {"workload": workload_text(args.config, spec, mr, len(blocks), None),
                    "voxel_updates_per_scan": sizes["vu_total"], "scans_per_s": 1.0 / cb["scan_seconds"],
                    "wall_s": wall,
                    "note": "reference CPU path as restated bit-exactly by the oracle port (the reference's "
@@ -521,8 +532,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic seeded helical phantom (config-2 geometry), generated on the device",
         "config": {
-            "workload": "%s: 736 ch x 32 rows phi+z FFS -> 1472 x 64, 1152 views/turn, pitch 0.8, 10 turns, "
-                        "512^2 x 96 slices (3 blocks) thickened to %d x 3 mm; adaptive filter on" % (args.config, n_final),
+            "workload": workload_text(args.config, spec, mr, len(blocks), n_final),
             "path": ("whole scan: the union of the blocks' pull windows (%d frames) adaptive-filtered, rebinned "
                      "and ramp-filtered once, each block backprojected from it (%s / %s)"
                      % (sizes["union_h2d_bytes"] // (4 * frame), dev_entry, host_entry)) if args.path == "scan" else
