@@ -258,13 +258,18 @@ constexpr int kViewsPerThread = 8;
 // both hold fewer than 2^31 samples).
 // --------------------------------------------------------------------------
 
+// Raw rows per thread: the view-axis taps of a (channel, view) are computed
+// once and used for every row of the group.
+constexpr int kRowsPerThread = 8;
+
 // no-FFS and z-FFS: bilinear in (channel, view).  grid: x channel blocks,
-// y raw row, z chunks of kViewsPerThread views.
+// y groups of kRowsPerThread raw rows, z chunks of kViewsPerThread views.
 template <class Idx>
 __global__ void rebin_bilinear_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    int row = blockIdx.y;
+    int r0 = blockIdx.y * kRowsPerThread;
+    int r1 = min(r0 + kRowsPerThread, p.R_raw);
     int v0 = p.v_begin + blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
     const Idx frame_stride = (Idx)p.R_raw * p.N;
@@ -274,11 +279,7 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
         const float t_alpha = p.focal[s * p.Nos + c].t_alpha;
         const float t_off = p.n_ffs == 1 ? 0.0f : p.focal_offset[s];
         const float omu = tap.one_minus_u, u = tap.u;
-        int out_row = row;
-        if (p.n_ffs == 2) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
-        const float *base = p.raw + (Idx)row * p.N + s * frame_stride;
-        float *out = p.out + (Idx)out_row * nos + c;
-#pragma unroll 4
+        const float *base = p.raw + s * frame_stride;
         for (int v = v0; v < min(v0 + kViewsPerThread, p.v_end); ++v) {
             float alpha = focal_alpha(p.n_ffs, v + p.add, t_alpha, t_off, s);
             int i0, i1;
@@ -286,14 +287,21 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
             view_taps(alpha, p.n_proj, &i0, &i1, &w);
             const float *f0 = base + (Idx)(p.n_ffs * i0) * frame_stride;
             const float *f1 = base + (Idx)(p.n_ffs * i1) * frame_stride;
-            float a1 = __ldg(f0 + tap.i0), a2 = __ldg(f0 + tap.i1);
-            float a5 = __ldg(f1 + tap.i0), a6 = __ldg(f1 + tap.i1);
             float omw = __fsub_rn(1.0f, w);
-            float t1 = __fmul_rn(__fmul_rn(a1, omu), omw);
-            float t2 = __fmul_rn(__fmul_rn(a2, u), omw);
-            float t5 = __fmul_rn(__fmul_rn(a5, omu), w);
-            float t6 = __fmul_rn(__fmul_rn(a6, u), w);
-            out[(Idx)v * p.R * nos] = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t5), t6);
+            float *out_v = p.out + (Idx)v * p.R * nos + c;
+#pragma unroll 4
+            for (int row = r0; row < r1; ++row) {
+                const Idx ro = (Idx)row * p.N;
+                float a1 = __ldg(f0 + ro + tap.i0), a2 = __ldg(f0 + ro + tap.i1);
+                float a5 = __ldg(f1 + ro + tap.i0), a6 = __ldg(f1 + ro + tap.i1);
+                float t1 = __fmul_rn(__fmul_rn(a1, omu), omw);
+                float t2 = __fmul_rn(__fmul_rn(a2, u), omw);
+                float t5 = __fmul_rn(__fmul_rn(a5, omu), w);
+                float t6 = __fmul_rn(__fmul_rn(a6, u), w);
+                int out_row = row;
+                if (p.n_ffs == 2) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
+                out_v[(Idx)out_row * nos] = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t5), t6);
+            }
         }
     }
 }
@@ -306,7 +314,8 @@ template <class Idx>
 __global__ void rebin_two_stage_kernel(RebinParams p)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    int row = blockIdx.y;
+    int r0 = blockIdx.y * kRowsPerThread;
+    int r1 = min(r0 + kRowsPerThread, p.R_raw);
     int v0 = p.v_begin + blockIdx.z * kViewsPerThread;
     if (c >= p.Nos) return;
     const Idx frame_stride = (Idx)p.R_raw * p.N;
@@ -319,23 +328,29 @@ __global__ void rebin_two_stage_kernel(RebinParams p)
         int q1 = qb + (tap.i1 & 1), ch1 = tap.i1 >> 1;
         const float ta0 = p.focal[q0 * p.N + ch0].t_alpha, to0 = p.focal_offset[q0];
         const float ta1 = p.focal[q1 * p.N + ch1].t_alpha, to1 = p.focal_offset[q1];
-        const float *b0 = p.raw + (Idx)row * p.N + ch0 + q0 * frame_stride;
-        const float *b1 = p.raw + (Idx)row * p.N + ch1 + q1 * frame_stride;
-        int out_row = row;
-        if (p.n_ffs == 4) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
-        float *out = p.out + (Idx)out_row * nos + c;
-#pragma unroll 4
+        const float *b0 = p.raw + ch0 + q0 * frame_stride;
+        const float *b1 = p.raw + ch1 + q1 * frame_stride;
         for (int v = v0; v < min(v0 + kViewsPerThread, p.v_end); ++v) {
             int proj = v + p.add;
-            int i0, i1;
+            int i0, i1, j0, j1;
             float w0, w1;
             view_taps(focal_alpha(p.n_ffs, proj, ta0, to0, q0), p.n_proj, &i0, &i1, &w0);
-            float T0 = __fadd_rn(__fmul_rn(__ldg(b0 + (Idx)(p.n_ffs * i0) * frame_stride), __fsub_rn(1.0f, w0)),
-                                 __fmul_rn(__ldg(b0 + (Idx)(p.n_ffs * i1) * frame_stride), w0));
-            view_taps(focal_alpha(p.n_ffs, proj, ta1, to1, q1), p.n_proj, &i0, &i1, &w1);
-            float T1 = __fadd_rn(__fmul_rn(__ldg(b1 + (Idx)(p.n_ffs * i0) * frame_stride), __fsub_rn(1.0f, w1)),
-                                 __fmul_rn(__ldg(b1 + (Idx)(p.n_ffs * i1) * frame_stride), w1));
-            out[(Idx)v * p.R * nos] = __fadd_rn(__fmul_rn(T0, tap.one_minus_u), __fmul_rn(T1, tap.u));
+            view_taps(focal_alpha(p.n_ffs, proj, ta1, to1, q1), p.n_proj, &j0, &j1, &w1);
+            const float *f00 = b0 + (Idx)(p.n_ffs * i0) * frame_stride;
+            const float *f01 = b0 + (Idx)(p.n_ffs * i1) * frame_stride;
+            const float *f10 = b1 + (Idx)(p.n_ffs * j0) * frame_stride;
+            const float *f11 = b1 + (Idx)(p.n_ffs * j1) * frame_stride;
+            const float omw0 = __fsub_rn(1.0f, w0), omw1 = __fsub_rn(1.0f, w1);
+            float *out_v = p.out + (Idx)v * p.R * nos + c;
+#pragma unroll 4
+            for (int row = r0; row < r1; ++row) {
+                const Idx ro = (Idx)row * p.N;
+                float T0 = __fadd_rn(__fmul_rn(__ldg(f00 + ro), omw0), __fmul_rn(__ldg(f01 + ro), w0));
+                float T1 = __fadd_rn(__fmul_rn(__ldg(f10 + ro), omw1), __fmul_rn(__ldg(f11 + ro), w1));
+                int out_row = row;
+                if (p.n_ffs == 4) out_row = 2 * row + (p.reverse_rows ? 1 - s : s);
+                out_v[(Idx)out_row * nos] = __fadd_rn(__fmul_rn(T0, tap.one_minus_u), __fmul_rn(T1, tap.u));
+            }
         }
     }
 }
@@ -373,7 +388,8 @@ int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float 
     p.v_begin = v_begin;
     p.v_end = v_end;
     int chunks = (v_end - v_begin + kViewsPerThread - 1) / kViewsPerThread;
-    if (chunks > 65535 || t.n_rows_raw > 65535) {
+    int row_groups = (t.n_rows_raw + kRowsPerThread - 1) / kRowsPerThread;
+    if (chunks > 65535 || row_groups > 65535) {
         set_error("rebin: %d views / %d rows exceed the launch grid", t.n_views, t.n_rows_raw);
         return CTBB_ERR_ARGUMENT;
     }
@@ -381,7 +397,7 @@ int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float 
     size_t n_out = (size_t)t.n_views * t.n_rows * t.n_os;
     bool narrow = n_raw < ((size_t)1 << 31) && n_out < ((size_t)1 << 31);
     dim3 block(128);
-    dim3 grid((t.n_os + 127) / 128, t.n_rows_raw, chunks);
+    dim3 grid((t.n_os + 127) / 128, row_groups, chunks);
     bool bilinear = t.mode == RebinMode::kNoFfs || t.mode == RebinMode::kZFfs;
     if (bilinear && narrow) rebin_bilinear_kernel<int><<<grid, block, 0, stream>>>(p);
     else if (bilinear) rebin_bilinear_kernel<size_t><<<grid, block, 0, stream>>>(p);
