@@ -96,6 +96,21 @@ def block_plans(mr):
     return out
 
 
+def max_over_ranks(ms, dist, device="cuda"):
+    """The slowest rank's time: every replica's step ends when the last one does."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(seed, rank):
+    """Each replica reconstructs its own seeded scan."""
+    return seed + 7919 * rank
+
+
 def workload_text(name, spec, mr, n_blocks, n_final):
     """One line naming the workload by its sizes."""
     ffs = {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(spec.z_ffs, spec.phi_ffs)]
@@ -358,7 +373,7 @@ def run_ours(args):
     objs = scans.phantom_objects(spec)
     d_scan = torch.empty(n * frame, dtype=torch.float32, device="cuda")
     L.call("ctbb_phantom_project_device", C.byref(mr), objs, len(objs), C.c_void_p(ta.data_ptr()),
-           C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), spec.seed + 7919 * rank,
+           C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), replica_seed(spec.seed, rank),
            C.c_void_p(d_scan.data_ptr()))
     d_final = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
 
@@ -401,10 +416,7 @@ def run_ours(args):
     per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
     ms = total_ms / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     value = world * sizes["vu_total"] / (ms * 1e-3)
 
     # e2e through the host-buffer entry point (pinned host scan and stack)
@@ -430,10 +442,7 @@ def run_ours(args):
             e2e_step()
         torch.cuda.synchronize()
         e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-        if dist is not None:
-            t = torch.tensor([e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
+        e_ms = max_over_ranks(e_ms, dist)
         same = bool(torch.equal(h_final.cuda(), d_final))
         e2e = {"value": world * sizes["vu_total"] / (e_ms * 1e-3), "unit": "voxel-updates/s",
                "h2d_bytes_per_step": sizes[h2d_key[args.path]], "d2h_bytes_per_step": n_final * plane * 4,
@@ -453,10 +462,7 @@ def run_ours(args):
                 ws_host_step()
             torch.cuda.synchronize()
             ws_e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-            if dist is not None:
-                t = torch.tensor([ws_e_ms], device="cuda")
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                ws_e_ms = float(t.item())
+            ws_e_ms = max_over_ranks(ws_e_ms, dist)
             ws_e2e = {"value": world * sizes["vu_total"] / (ws_e_ms * 1e-3), "unit": "voxel-updates/s",
                       "h2d_bytes_per_step": sizes[h2d_key[other_path]], "d2h_bytes_per_step": n_final * plane * 4,
                       "ms_per_step": ws_e_ms, "entry_point": alt_host}

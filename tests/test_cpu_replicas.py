@@ -1,0 +1,56 @@
+"""CPU tests of bench.py's multi-replica path (one process per GPU under
+torchrun): the slowest rank's time is what every rank reports, each replica
+reconstructs its own seeded scan, and the reference arm runs on rank 0 only.
+The ranks here are gloo processes on the host; no GPU is used."""
+import ast
+import os
+import subprocess
+import sys
+
+import pytest
+
+from tests.conftest import REPO
+
+torch = pytest.importorskip("torch")
+dist = pytest.importorskip("torch.distributed")
+
+
+def _rank_main(rank, world, port, out_path):
+    sys.path.insert(0, REPO)
+    import torch.distributed as d
+
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    d.init_process_group("gloo", rank=rank, world_size=world)
+    local_ms = [12.5, 40.25][rank]
+    slowest = bench.max_over_ranks(local_ms, d, device="cpu")
+    seed = bench.replica_seed(1234, rank)
+    gathered = [None] * world
+    d.all_gather_object(gathered, seed)
+    d.barrier()
+    d.destroy_process_group()
+    with open("%s.%d" % (out_path, rank), "w") as f:
+        f.write("%r %r\n" % (slowest, gathered))
+
+
+def test_max_over_ranks_and_seeds_with_two_gloo_ranks(tmp_path):
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = str(tmp_path / "rank")
+    mp.start_processes(_rank_main, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
+    for r in range(2):
+        slowest, seeds = open("%s.%d" % (out, r)).read().split(" ", 1)
+        assert float(slowest) == 40.25
+        seeds = ast.literal_eval(seeds.strip())
+        assert len(set(seeds)) == 2  # each replica its own scan
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip() == ""
