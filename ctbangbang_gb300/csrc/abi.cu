@@ -69,6 +69,7 @@ struct Context {
     RampFilterPlan ramp;
     void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
     int sms = 0;
+    std::atomic<int> device{-1};  // the device the work buffers live on (-1: none yet)
     // host-buffer whole-scan path: second window buffer and a copy stream
     DeviceBuffer raw_in2;
     cudaStream_t copy_stream = nullptr;
@@ -198,6 +199,17 @@ int require_device()
                   e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
         return CTBB_ERR_NO_DEVICE;
     }
+    // the work buffers, tables and streams belong to the device of the first
+    // call; another device must not reach them
+    int dev = 0;
+    CTBB_CUDA_TRY(cudaGetDevice(&dev));
+    Context &c = ctx();
+    int bound = -1;
+    if (!c.device.compare_exchange_strong(bound, dev) && bound != dev) {
+        set_error("the library's work buffers live on device %d, the current device is %d: call "
+                  "ctbb_release_workspace() before switching devices", bound, dev);
+        return CTBB_ERR_STATE;
+    }
     return CTBB_OK;
 }
 
@@ -280,13 +292,32 @@ extern "C" int ctbb_release_workspace(void)
 {
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
-    for (DeviceBuffer *b : {&c.raw_in, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack, &c.scratch,
-                            &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices, &c.fin_weights})
+    // release on the device the buffers belong to
+    int cur = 0, bound = c.device.load();
+    cudaGetDevice(&cur);
+    if (bound >= 0 && bound != cur) cudaSetDevice(bound);
+    if (bound >= 0) cudaDeviceSynchronize();
+    for (DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
+                            &c.scratch, &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices, &c.fin_weights})
         b->release();
     if (c.rebin_tables.base) cudaFree(c.rebin_tables.base);
     c.rebin_tables = DeviceRebinTables{};
     if (c.ramp.d_spectrum) cudaFree(c.ramp.d_spectrum);
     c.ramp = RampFilterPlan{};
+    if (c.copy_stream) {
+        for (int i = 0; i < 2; ++i) {
+            cudaEventDestroy(c.copied[i]);
+            cudaEventDestroy(c.consumed[i]);
+            c.copied[i] = c.consumed[i] = nullptr;
+        }
+        for (cudaEvent_t e : c.chunk_copied) cudaEventDestroy(e);
+        c.chunk_copied.clear();
+        cudaStreamDestroy(c.copy_stream);
+        c.copy_stream = nullptr;
+    }
+    c.sms = 0;
+    c.device.store(-1);
+    if (bound >= 0 && bound != cur) cudaSetDevice(cur);
     return CTBB_OK;
 }
 

@@ -19,6 +19,7 @@
 // one write of the rows; the transform lives in shared memory.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -540,8 +541,12 @@ int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_line
     p.spectrum = plan.d_spectrum;
     auto padded = [](size_t m) { return m + ((m - 1) >> 4) + 1; };
     size_t smem = sizeof(float2) * 2 * padded((size_t)p.m);
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory limits are a per-device setting of each kernel
+    static std::atomic<uint64_t> attr_devices{0};
+    int dev = 0;
+    CTBB_CUDA_TRY(cudaGetDevice(&dev));
+    const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
+    if (!bit || !(attr_devices.load() & bit)) {
         size_t max_smem = sizeof(float2) * 2 * padded(kMaxRampTransform);
         CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)max_smem));
@@ -549,7 +554,7 @@ int launch_ramp_filter(const RampFilterPlan &plan, float *d_lines, size_t n_line
                                            (int)(sizeof(float2) * 2 * padded(kM4096))));
         CTBB_CUDA_TRY(cudaFuncSetAttribute(ramp_fft4096_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(sizeof(float2) * 2 * padded(kM4096))));
-        attr_set = true;
+        attr_devices.fetch_or(bit);
     }
     int per_sm = (int)std::max<size_t>(1, (size_t)(220 * 1024) / smem);
     if (per_sm > 4) per_sm = 4;

@@ -384,7 +384,11 @@ double ctbb_fp32_peak_tflops(int repeats);
 /* Bytes of device workspace ctbb_reconstruct_device keeps for this plan. */
 size_t ctbb_workspace_bytes(const struct recon_metadata *mr);
 
-/* Release every cached device buffer of the library. */
+/* Release every cached device buffer, table, copy stream and event of the
+   library (on the device they belong to) and unbind it from that device.
+   The library's work buffers live on the device that was current at the
+   first compute call; a call while another device is current returns
+   CTBB_ERR_STATE until this function has been called. */
 int ctbb_release_workspace(void);
 
 /* Number of kernels this library launched since load (all entry points). */

@@ -374,3 +374,30 @@ def test_whole_scan_streamed_from_host_equals_device_path(torch_cuda, lib, tmp_p
     np.testing.assert_array_equal(h_final, d_fin.cpu().numpy())
     other.close()
     scan.close()
+
+
+def test_release_workspace_then_reconstruct_again(torch_cuda, lib, tmp_path):
+    """ctbb_release_workspace frees every cached buffer, table, stream and
+    event and unbinds the device; the next call rebuilds them and gives the
+    same stack, on the block loop and on the streamed whole-scan path."""
+    torch = torch_cuda
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=46)
+    scan = H.Scan(spec, str(tmp_path))
+    mr = scan.mr
+    n_final = lib.ctbb_n_slices_final(C.byref(mr))
+    plane = mr.rp.nx * mr.rp.ny
+    d_scan = dev(torch, scan.frames.reshape(-1))
+    h_scan = np.ascontiguousarray(scan.frames.reshape(-1), dtype=np.float32)
+    first = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_device", C.byref(mr), ptr(d_scan), ptr(first), 0.0)
+    h_first = np.zeros(n_final * plane, np.float32)
+    L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(h_scan), fptr(h_first), 0.0)
+    torch.cuda.synchronize()
+    L.call("ctbb_release_workspace")
+    again = torch.empty_like(first)
+    L.call("ctbb_reconstruct_device", C.byref(mr), ptr(d_scan), ptr(again), 0.0)
+    h_again = np.zeros_like(h_first)
+    L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(h_scan), fptr(h_again), 0.0)
+    np.testing.assert_array_equal(again.cpu().numpy(), first.cpu().numpy())
+    np.testing.assert_array_equal(h_again, h_first)
+    scan.close()
