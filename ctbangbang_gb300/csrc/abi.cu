@@ -9,7 +9,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <condition_variable>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "adaptive_filter.h"
@@ -75,6 +78,10 @@ struct Context {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> chunk_copied;  // whole-scan host path: one per chunk
+    // whole-scan file path: two pinned staging buffers and their reuse events
+    void *stage[2] = {nullptr, nullptr};
+    size_t stage_bytes = 0;
+    cudaEvent_t stage_free[2] = {nullptr, nullptr};
     // per-stage CUDA-event timing (ctbb_profile_*)
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> open_events[kProfileStages];
@@ -312,6 +319,13 @@ extern "C" int ctbb_release_workspace(void)
         }
         for (cudaEvent_t e : c.chunk_copied) cudaEventDestroy(e);
         c.chunk_copied.clear();
+        for (int i = 0; i < 2; ++i) {
+            if (c.stage_free[i]) cudaEventDestroy(c.stage_free[i]);
+            if (c.stage[i]) cudaFreeHost(c.stage[i]);
+            c.stage_free[i] = nullptr;
+            c.stage[i] = nullptr;
+        }
+        c.stage_bytes = 0;
         cudaStreamDestroy(c.copy_stream);
         c.copy_stream = nullptr;
     }
@@ -711,27 +725,59 @@ static int ensure_copy_stream(Context &c)
     return CTBB_OK;
 }
 
-// Whole scan from host buffers, streamed: the union window is copied in
-// chunks on the copy stream while, on the compute stream, each arriving chunk
-// advances the adaptive filter as far as its statistics windows allow, the
-// views whose frames are final are rebinned and ramp-filtered, and every
-// block whose views are all ready is backprojected.  Same kernels on the same
-// data as ctbb_reconstruct_scan_device, so the same result.
-extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
-                                          float mu_water)
-{
-    clear_error();
-    if (!mr || !h_scan || !h_final || !mr->table_positions) {
-        set_error("ctbb_reconstruct_scan_host: metadata not configured or null buffer");
-        return CTBB_ERR_ARGUMENT;
+// Where the streamed whole-scan path gets the union window's frames: begin()
+// starts the copies of all chunks (each recording chunk_copied[k] on the copy
+// stream once its frames are enqueued), issued(k) returns once chunk k's
+// copies and event are enqueued, finish() ends any helper thread.
+struct ChunkFeed {
+    virtual ~ChunkFeed() = default;
+    virtual int begin(Context &c, long long g0, long long g1, int chunk, int n_chunks, float *d_raw) = 0;
+    virtual int issued(int k) = 0;
+    virtual int finish() = 0;
+};
+
+// frames [a, e) of the scan from a host array of n_readings frames; frames
+// outside [0, n_readings) are zeros
+struct HostFeed : ChunkFeed {
+    const float *h_scan;
+    long long n_readings;
+    size_t frame;
+    HostFeed(const float *h, long long n, size_t f) : h_scan(h), n_readings(n), frame(f) {}
+    int begin(Context &c, long long g0, long long g1, int chunk, int n_chunks, float *d_raw) override
+    {
+        for (int k = 0; k < n_chunks; ++k) {
+            long long a = g0 + (long long)k * chunk, e = std::min(g1, a + chunk);
+            long long da = std::max(a, 0LL), de = std::min(e, n_readings);
+            float *dst = d_raw + (size_t)(a - g0) * frame;
+            if (de <= da) {
+                CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(e - a) * frame * sizeof(float), c.copy_stream));
+            } else {
+                if (da > a)
+                    CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(da - a) * frame * sizeof(float), c.copy_stream));
+                CTBB_CUDA_TRY(cudaMemcpyAsync(d_raw + (size_t)(da - g0) * frame, h_scan + (size_t)da * frame,
+                                              (size_t)(de - da) * frame * sizeof(float), cudaMemcpyHostToDevice,
+                                              c.copy_stream));
+                if (e > de)
+                    CTBB_CUDA_TRY(cudaMemsetAsync(d_raw + (size_t)(de - g0) * frame, 0,
+                                                  (size_t)(e - de) * frame * sizeof(float), c.copy_stream));
+            }
+            CTBB_CUDA_TRY(cudaEventRecord(c.chunk_copied[k], c.copy_stream));
+        }
+        return CTBB_OK;
     }
-    CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
-    std::lock_guard<std::mutex> lk(c.mu);
+    int issued(int) override { return CTBB_OK; }
+    int finish() override { return CTBB_OK; }
+};
+
+// Whole scan, streamed: each chunk of the union window, once its frames are
+// on the device, advances the adaptive filter as far as its statistics
+// windows allow; the views whose frames are final are rebinned and
+// ramp-filtered, and every block whose views are all ready is backprojected.
+// Same kernels on the same data as ctbb_reconstruct_scan_device, so the same
+// result.  The caller holds c.mu.
+static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed, float *h_final, float mu_water)
+{
     CTBB_TRY(ensure_copy_stream(c));
-    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
-    const long long n_readings = (long long)mr->rp.n_readings;
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     const size_t n_block = mr->ri.n_slices_block;
     std::vector<struct recon_info> blocks;
@@ -761,44 +807,33 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
     CTBB_CUDA_TRY(cudaEventRecord(c.consumed[0], c.stream));
     CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[0], 0));
     float *d_raw = c.raw_in.as<float>();
-    for (int k = 0; k < n_chunks; ++k) {
-        long long a = g0 + (long long)k * chunk, e = std::min(g1, a + chunk);
-        long long da = std::max(a, 0LL), de = std::min(e, n_readings);
-        float *dst = d_raw + (size_t)(a - g0) * frame;
-        if (de <= da) {
-            CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(e - a) * frame * sizeof(float), c.copy_stream));
-        } else {
-            if (da > a) CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(da - a) * frame * sizeof(float), c.copy_stream));
-            CTBB_CUDA_TRY(cudaMemcpyAsync(d_raw + (size_t)(da - g0) * frame, h_scan + (size_t)da * frame,
-                                          (size_t)(de - da) * frame * sizeof(float), cudaMemcpyHostToDevice,
-                                          c.copy_stream));
-            if (e > de)
-                CTBB_CUDA_TRY(cudaMemsetAsync(d_raw + (size_t)(de - g0) * frame, 0,
-                                              (size_t)(e - de) * frame * sizeof(float), c.copy_stream));
-        }
-        CTBB_CUDA_TRY(cudaEventRecord(c.chunk_copied[k], c.copy_stream));
-    }
+    int status = feed.begin(c, g0, g1, chunk, n_chunks, d_raw);
     // per-scan tables, once
     RebinTables rt;
-    CTBB_TRY(build_rebin_tables(mg, &rt));
-    CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
-    {
-        std::vector<float> taps(2 * dg.n_os);
-        CTBB_TRY(ctbb_load_filter(&mg, taps.data()));
-        CTBB_TRY(prepare_ramp_filter(taps.data(), (int)dg.n_os, &c.ramp, c.stream));
-    }
+    std::vector<float> taps(2 * dg.n_os);
+    if (status == CTBB_OK) status = build_rebin_tables(mg, &rt);
+    if (status == CTBB_OK) status = upload_rebin_tables(rt, &c.rebin_tables, c.stream);
+    if (status == CTBB_OK) status = ctbb_load_filter(&mg, taps.data());
+    if (status == CTBB_OK) status = prepare_ramp_filter(taps.data(), (int)dg.n_os, &c.ramp, c.stream);
     AfStream af(mg);
     const size_t view_elems = dg.n_rows * dg.n_os;
     const int V = (int)dg.n_views;
     int v_done = 0;
     size_t b_done = 0;
-    for (int k = 0; k < n_chunks; ++k) {
-        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.chunk_copied[k], 0));
+    for (int k = 0; k < n_chunks && status == CTBB_OK; ++k) {
+        status = feed.issued(k);
+        if (status != CTBB_OK) break;
+        status = cudaStreamWaitEvent(c.stream, c.chunk_copied[k], 0) == cudaSuccess ? CTBB_OK : CTBB_ERR_CUDA;
+        if (status != CTBB_OK) {
+            set_error("scan: cudaStreamWaitEvent failed");
+            break;
+        }
         int arrived = std::min(G, (k + 1) * chunk);
         {
             StageScope scope(c, 0);
-            CTBB_TRY(af.advance(mg, d_raw, c.raw_filt.as<float>(), c.scratch.as<float>(), arrived, c.stream));
+            status = af.advance(mg, d_raw, c.raw_filt.as<float>(), c.scratch.as<float>(), arrived, c.stream);
         }
+        if (status != CTBB_OK) break;
         // views whose frames are all final
         int v_ready = V;
         if (af.filtered() < G) {
@@ -808,18 +843,20 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
         if (v_ready > v_done) {
             {
                 StageScope scope(c, 1);
-                CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream,
-                                      v_done, v_ready));
+                status = launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream,
+                                      v_done, v_ready);
             }
+            if (status != CTBB_OK) break;
             {
                 StageScope scope(c, 2);
-                CTBB_TRY(launch_ramp_filter(c.ramp, c.rebin.as<float>() + (size_t)v_done * view_elems,
-                                            (size_t)(v_ready - v_done) * dg.n_rows, c.stream));
+                status = launch_ramp_filter(c.ramp, c.rebin.as<float>() + (size_t)v_done * view_elems,
+                                            (size_t)(v_ready - v_done) * dg.n_rows, c.stream);
             }
+            if (status != CTBB_OK) break;
             v_done = v_ready;
         }
         // blocks whose views (i + k n_half, k < nht) are all ready
-        while (b_done < blocks.size()) {
+        while (b_done < blocks.size() && status == CTBB_OK) {
             struct recon_metadata mb = *mr;
             mb.ri = blocks[b_done];
             BlockDims db = block_dims(mb);
@@ -828,14 +865,16 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
             if (need > (size_t)v_done && v_done < V) break;
             mr->ri = blocks[b_done];
             float *slab = c.image.as<float>() + b_done * n_block * plane;
-            CTBB_TRY(do_backproject(*mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
-                                    slab));
+            status = do_backproject(*mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
+                                    slab);
             ++b_done;
         }
     }
+    int fs = feed.finish();
+    if (status != CTBB_OK) return status;
+    if (fs != CTBB_OK) return fs;
     if (b_done != blocks.size()) {
-        set_error("ctbb_reconstruct_scan_host: %zu of %zu blocks left unfinished", blocks.size() - b_done,
-                  blocks.size());
+        set_error("whole scan: %zu of %zu blocks left unfinished", blocks.size() - b_done, blocks.size());
         return CTBB_ERR_STATE;
     }
     CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
@@ -843,6 +882,164 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
                                   cudaMemcpyDeviceToHost, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
+}
+
+// Whole scan from host buffers, streamed: the union window is copied in
+// chunks on the copy stream while the compute stream works on the chunks
+// that have arrived (scan_streamed).  Same result as
+// ctbb_reconstruct_scan_device.
+extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                                          float mu_water)
+{
+    clear_error();
+    if (!mr || !h_scan || !h_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_scan_host: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    HostFeed feed(h_scan, (long long)mr->rp.n_readings, mr->cg.n_rows_raw * mr->cg.n_channels);
+    return scan_streamed(c, mr, feed, h_final, mu_water);
+}
+
+// Frames [a, e) of the scan read from a FileType 0 raw file -- frame i at
+// byte raw_data_offset + i * frame_bytes, frames before the start or past the
+// end of the file read as zeros, as extract_projections reads them.  A reader
+// thread fills two pinned staging buffers in turn and enqueues each chunk's
+// host->device copy itself, so the copies never wait for the compute loop.
+struct FileFeed : ChunkFeed {
+    std::string path;
+    long long offset;
+    size_t frame;
+    std::thread reader;
+    std::mutex mu;
+    std::condition_variable cv;
+    int n_issued = 0;
+    bool stop = false;  // set by finish(): no further chunks
+    int status = CTBB_OK;
+    std::string error;
+    FileFeed(std::string p, long long off, size_t f) : path(std::move(p)), offset(off), frame(f) {}
+    ~FileFeed() override
+    {
+        if (reader.joinable()) reader.join();
+    }
+    void fail(const char *what)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (status == CTBB_OK) {
+            status = CTBB_ERR_IO;
+            error = what;
+        }
+        cv.notify_all();
+    }
+    int begin(Context &c, long long g0, long long g1, int chunk, int n_chunks, float *d_raw) override
+    {
+        const size_t need = (size_t)chunk * frame * sizeof(float);
+        if (c.stage_bytes < need) {
+            for (int i = 0; i < 2; ++i) {
+                if (c.stage[i]) cudaFreeHost(c.stage[i]);
+                c.stage[i] = nullptr;
+            }
+            c.stage_bytes = 0;
+            for (int i = 0; i < 2; ++i) CTBB_CUDA_TRY(cudaHostAlloc(&c.stage[i], need, cudaHostAllocDefault));
+            c.stage_bytes = need;
+        }
+        for (int i = 0; i < 2; ++i) {
+            if (!c.stage_free[i]) CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.stage_free[i], cudaEventDisableTiming));
+            CTBB_CUDA_TRY(cudaEventRecord(c.stage_free[i], c.copy_stream));
+        }
+        FILE *f = fopen(path.c_str(), "rb");
+        if (!f) {
+            set_error("raw data file %s not found", path.c_str());
+            return CTBB_ERR_IO;
+        }
+        int dev = 0;
+        CTBB_CUDA_TRY(cudaGetDevice(&dev));
+        reader = std::thread([this, &c, f, g0, g1, chunk, n_chunks, d_raw, dev] {
+            cudaSetDevice(dev);
+            for (int k = 0; k < n_chunks; ++k) {
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (stop || status != CTBB_OK) break;
+                }
+                int slot = k & 1;
+                if (cudaEventSynchronize(c.stage_free[slot]) != cudaSuccess) {
+                    fail("staging buffer wait failed");
+                    break;
+                }
+                long long a = g0 + (long long)k * chunk, e = std::min(g1, a + chunk);
+                float *stage = static_cast<float *>(c.stage[slot]);
+                size_t n = (size_t)(e - a) * frame;
+                memset(stage, 0, n * sizeof(float));
+                long long ra = std::max(a, 0LL);
+                if (e > ra) {
+                    long long pos = offset + ra * (long long)(frame * sizeof(float));
+                    if (fseeko(f, (off_t)pos, SEEK_SET) == 0) {
+                        size_t got = fread(stage + (size_t)(ra - a) * frame, sizeof(float), (size_t)(e - ra) * frame, f);
+                        (void)got;  // frames past the end of the file stay zero
+                    }
+                }
+                if (cudaMemcpyAsync(d_raw + (size_t)(a - g0) * frame, stage, n * sizeof(float),
+                                    cudaMemcpyHostToDevice, c.copy_stream) != cudaSuccess ||
+                    cudaEventRecord(c.stage_free[slot], c.copy_stream) != cudaSuccess ||
+                    cudaEventRecord(c.chunk_copied[k], c.copy_stream) != cudaSuccess) {
+                    fail("host->device copy of a raw chunk failed");
+                    break;
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                n_issued = k + 1;
+                cv.notify_all();
+            }
+            fclose(f);
+        });
+        return CTBB_OK;
+    }
+    int issued(int k) override
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return n_issued > k || status != CTBB_OK; });
+        if (n_issued > k) return CTBB_OK;
+        set_error("%s", error.c_str());
+        return status;
+    }
+    int finish() override
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;  // the compute loop is done with the chunks (or gave up)
+        }
+        if (reader.joinable()) reader.join();
+        std::lock_guard<std::mutex> lk(mu);
+        if (status != CTBB_OK) set_error("%s", error.c_str());
+        return status;
+    }
+};
+
+// Whole scan straight from the raw file (FileType 0): the file is read in
+// chunks while earlier chunks are copied and processed (scan_streamed).
+// Same result as ctbb_reconstruct_scan_device on the file's frames.
+extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float mu_water)
+{
+    clear_error();
+    if (!mr || !h_final || !mr->table_positions) {
+        set_error("ctbb_reconstruct_scan_file: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    if (mr->rp.file_type != 0) {
+        set_error("ctbb_reconstruct_scan_file: FileType %d is not read here (only 0, float32 frames)",
+                  mr->rp.file_type);
+        return CTBB_ERR_CONFIG;
+    }
+    CTBB_TRY(check_mr(mr));
+    CTBB_TRY(require_device());
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    char path[4096 + 255 + 2];
+    snprintf(path, sizeof(path), "%s/%s", mr->rp.raw_data_dir, mr->rp.raw_data_file);
+    FileFeed feed(path, (long long)mr->rp.raw_data_offset, mr->cg.n_rows_raw * mr->cg.n_channels);
+    return scan_streamed(c, mr, feed, h_final, mu_water);
 }
 
 extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,

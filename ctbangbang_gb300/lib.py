@@ -50,6 +50,7 @@ PROTOTYPES = {
     "ctbb_reconstruct_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
     "ctbb_reconstruct_scan_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
     "ctbb_reconstruct_scan_host": (C.c_int, [_MR, _F, _F, C.c_float]),
+    "ctbb_reconstruct_scan_file": (C.c_int, [_MR, _F, C.c_float]),
     "ctbb_reconstruct_host": (C.c_int, [_MR, _F, _F, C.c_float]),
     "ctbb_profile_enable": (C.c_int, [C.c_int]),
     "ctbb_profile_read": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int, C.c_int]),

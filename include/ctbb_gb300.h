@@ -362,6 +362,18 @@ int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan,
 int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan,
                                float *h_final, float mu_water);
 
+/* ctbb_reconstruct_scan_host reading the raw file of the plan itself (no
+   counterpart in the reference, whose extract_projections reads each
+   block's window again, src/setup.cu:681-767): a reader thread reads the
+   union window of <RawDataDir>/<RawDataFile> (FileType 0: float32 frames at
+   RawOffset + i * frame bytes; frames before the start or past the end of
+   the file are zeros) in chunks into two pinned staging buffers (kept by the
+   library, freed by ctbb_release_workspace) and enqueues each chunk's copy,
+   while the compute stream works on the chunks that have arrived.  Other
+   FileTypes return CTBB_ERR_CONFIG.  Same result as
+   ctbb_reconstruct_scan_device on the file's frames. */
+int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float mu_water);
+
 /* As ctbb_reconstruct_device from host buffers: each block's pull window is
    copied from h_scan [n_readings][n_rows_raw][n_channels] on a second stream
    (double-buffered, overlapping the previous block's compute when h_scan is

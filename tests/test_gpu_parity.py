@@ -401,3 +401,34 @@ def test_release_workspace_then_reconstruct_again(torch_cuda, lib, tmp_path):
     np.testing.assert_array_equal(again.cpu().numpy(), first.cpu().numpy())
     np.testing.assert_array_equal(h_again, h_first)
     scan.close()
+
+
+def test_whole_scan_from_raw_file_equals_device_path(torch_cuda, lib, tmp_path):
+    """ctbb_reconstruct_scan_file reads the plan's raw file in chunks on a
+    reader thread while the earlier chunks are processed: the same stack as
+    the device whole-scan path on the same frames, bit for bit.  The file is
+    cut 700 frames short, inside the last pull window, so the frames past its
+    end must read as zeros."""
+    torch = torch_cuda
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=47)
+    scan = H.Scan(spec, str(tmp_path))
+    mr = scan.mr
+    frames = scan.frames.reshape(spec.n_readings, -1).copy()
+    keep = spec.n_readings - 700
+    scans.write_raw(os.path.join(str(tmp_path), "scan.raw"), frames[:keep])
+    frames[keep:] = 0.0
+    n_final = lib.ctbb_n_slices_final(C.byref(mr))
+    plane = mr.rp.nx * mr.rp.ny
+    h_file = np.zeros(n_final * plane, np.float32)
+    L.call("ctbb_reconstruct_scan_file", C.byref(mr), fptr(h_file), 0.0)
+    s_last = int(mr.ri.idx_pull_start)  # the last block's window after the call
+    assert s_last < keep < s_last + mr.ri.n_proj_pull
+    d_scan = dev(torch, frames.reshape(-1))
+    d_fin = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_scan_device", C.byref(mr), ptr(d_scan), ptr(d_fin), 0.0)
+    np.testing.assert_array_equal(h_file, d_fin.cpu().numpy())
+    # a second call reuses the staging buffers
+    h_again = np.zeros_like(h_file)
+    L.call("ctbb_reconstruct_scan_file", C.byref(mr), fptr(h_again), 0.0)
+    np.testing.assert_array_equal(h_again, h_file)
+    scan.close()
