@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--file", action="store_true",
+                    help="also time ctbb_reconstruct_scan_file on the scan written to the plan's raw file")
     ap.add_argument("--no-whole-scan", action="store_true",
                     help="skip the measurement of the other path (see --path)")
     ap.add_argument("--path", choices=["scan", "blocks"], default="scan",
@@ -422,6 +424,7 @@ def run_ours(args):
     # e2e through the host-buffer entry point (pinned host scan and stack)
     e2e = None
     ws_e2e = None
+    e2e_file = None
     if not args.no_e2e:
         h_scan = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
         h_scan.copy_(d_scan)
@@ -466,6 +469,29 @@ def run_ours(args):
             ws_e2e = {"value": world * sizes["vu_total"] / (ws_e_ms * 1e-3), "unit": "voxel-updates/s",
                       "h2d_bytes_per_step": sizes[h2d_key[other_path]], "d2h_bytes_per_step": n_final * plane * 4,
                       "ms_per_step": ws_e_ms, "entry_point": alt_host}
+        if args.file:
+            # the whole-scan path reading the plan's raw file (written once,
+            # outside the timed region; the file cache holds it afterwards)
+            raw_path = os.path.join(mr.rp.raw_data_dir.decode(), mr.rp.raw_data_file.decode())
+            h_scan.numpy().tofile(raw_path)
+
+            def file_step():
+                L.call("ctbb_reconstruct_scan_file", C.byref(mr), fp, C.c_float(0.0))
+
+            for _ in range(2):
+                file_step()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                file_step()
+            torch.cuda.synchronize()
+            f_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
+            e2e_file = {"value": world * sizes["vu_total"] / (f_ms * 1e-3), "unit": "voxel-updates/s",
+                        "read_bytes_per_step": sizes["union_h2d_bytes"], "ms_per_step": f_ms,
+                        "matches_device_path": bool(torch.equal(h_final.cuda(), d_final))
+                        if args.path == "scan" else None,
+                        "entry_point": "ctbb_reconstruct_scan_file"}
+            os.remove(raw_path)
         del h_scan, h_final
 
     # the other path (block loop or whole scan) on the same resident scan, and
@@ -562,6 +588,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "other_path": whole,
+        "e2e_file": e2e_file,
         "gpu_launches": launches / args.steps,
         "clocks": clk,
     }

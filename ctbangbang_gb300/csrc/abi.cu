@@ -3,6 +3,8 @@
 // semantics (host buffers in, host buffers out, d_rebin handed from rebin_filter
 // to backproject).
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <unistd.h>
 
 #include <atomic>
 #include <cstdio>
@@ -909,6 +911,8 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
 // end of the file read as zeros, as extract_projections reads them.  A reader
 // thread fills two pinned staging buffers in turn and enqueues each chunk's
 // host->device copy itself, so the copies never wait for the compute loop.
+constexpr int kReadThreads = 8;  // threads reading one chunk of the raw file
+
 struct FileFeed : ChunkFeed {
     std::string path;
     long long offset;
@@ -950,14 +954,14 @@ struct FileFeed : ChunkFeed {
             if (!c.stage_free[i]) CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.stage_free[i], cudaEventDisableTiming));
             CTBB_CUDA_TRY(cudaEventRecord(c.stage_free[i], c.copy_stream));
         }
-        FILE *f = fopen(path.c_str(), "rb");
-        if (!f) {
+        int fd = open(path.c_str(), O_RDONLY);
+        if (fd < 0) {
             set_error("raw data file %s not found", path.c_str());
             return CTBB_ERR_IO;
         }
         int dev = 0;
         CTBB_CUDA_TRY(cudaGetDevice(&dev));
-        reader = std::thread([this, &c, f, g0, g1, chunk, n_chunks, d_raw, dev] {
+        reader = std::thread([this, &c, fd, g0, g1, chunk, n_chunks, d_raw, dev] {
             cudaSetDevice(dev);
             for (int k = 0; k < n_chunks; ++k) {
                 {
@@ -972,15 +976,11 @@ struct FileFeed : ChunkFeed {
                 long long a = g0 + (long long)k * chunk, e = std::min(g1, a + chunk);
                 float *stage = static_cast<float *>(c.stage[slot]);
                 size_t n = (size_t)(e - a) * frame;
-                memset(stage, 0, n * sizeof(float));
                 long long ra = std::max(a, 0LL);
-                if (e > ra) {
-                    long long pos = offset + ra * (long long)(frame * sizeof(float));
-                    if (fseeko(f, (off_t)pos, SEEK_SET) == 0) {
-                        size_t got = fread(stage + (size_t)(ra - a) * frame, sizeof(float), (size_t)(e - ra) * frame, f);
-                        (void)got;  // frames past the end of the file stay zero
-                    }
-                }
+                if (ra > a) memset(stage, 0, (size_t)(ra - a) * frame * sizeof(float));  // before frame 0
+                if (e > ra) read_frames(fd, offset + ra * (long long)(frame * sizeof(float)),
+                                        reinterpret_cast<char *>(stage + (size_t)(ra - a) * frame),
+                                        (size_t)(e - ra) * frame * sizeof(float));
                 if (cudaMemcpyAsync(d_raw + (size_t)(a - g0) * frame, stage, n * sizeof(float),
                                     cudaMemcpyHostToDevice, c.copy_stream) != cudaSuccess ||
                     cudaEventRecord(c.stage_free[slot], c.copy_stream) != cudaSuccess ||
@@ -992,9 +992,33 @@ struct FileFeed : ChunkFeed {
                 n_issued = k + 1;
                 cv.notify_all();
             }
-            fclose(f);
+            close(fd);
         });
         return CTBB_OK;
+    }
+    // bytes [pos, pos + len) of the file into dst by several threads at once;
+    // what lies past the end of the file reads as zeros
+    static void read_frames(int fd, long long pos, char *dst, size_t len)
+    {
+        const size_t kSlice = (size_t)32 << 20;
+        size_t n_slices = (len + kSlice - 1) / kSlice;
+        int n_threads = (int)std::min<size_t>(n_slices, (size_t)kReadThreads);
+        std::atomic<size_t> next{0};
+        auto work = [&] {
+            for (size_t i = next++; i < n_slices; i = next++) {
+                size_t off = i * kSlice, want = std::min(kSlice, len - off), got = 0;
+                while (got < want) {
+                    ssize_t r = pread(fd, dst + off + got, want - got, (off_t)(pos + (long long)(off + got)));
+                    if (r <= 0) break;
+                    got += (size_t)r;
+                }
+                if (got < want) memset(dst + off + got, 0, want - got);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < n_threads; ++t) pool.emplace_back(work);
+        work();
+        for (auto &t : pool) t.join();
     }
     int issued(int k) override
     {
