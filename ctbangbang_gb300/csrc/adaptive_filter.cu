@@ -271,17 +271,29 @@ __global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
     const int n4 = (int)(frame / 4);
     if (threadIdx.x == 0) n_list = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-        float4 v = __ldg(src + i);
-        dst[i] = v;
-        if (v.x > T || v.y > T || v.z > T || v.w > T) {
-            float c[4] = {v.x, v.y, v.z, v.w};
+    // kUnroll independent 16-byte loads in flight per thread
+    constexpr int kUnroll = 4;
+    for (int i0 = threadIdx.x; i0 < n4; i0 += kUnroll * blockDim.x) {
+        float4 v[kUnroll];
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (c[e] > T) {
-                    int slot = atomicAdd(&n_list, 1);
-                    if (slot < kSmoothListMax) list[slot] = 4 * i + e;
-                }
+        for (int u = 0; u < kUnroll; ++u) {
+            int i = i0 + u * blockDim.x;
+            if (i < n4) v[u] = __ldg(src + i);
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            int i = i0 + u * blockDim.x;
+            if (i >= n4) break;
+            dst[i] = v[u];
+            if (v[u].x > T || v[u].y > T || v[u].z > T || v[u].w > T) {
+                float c[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (c[e] > T) {
+                        int slot = atomicAdd(&n_list, 1);
+                        if (slot < kSmoothListMax) list[slot] = 4 * i + e;
+                    }
+            }
         }
     }
     __syncthreads();
