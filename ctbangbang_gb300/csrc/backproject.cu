@@ -19,11 +19,18 @@
 // interpolation) use FMA and reciprocals.  The reference's pi' = 3.1415368979f
 // is used where it uses it.
 //
-// GB300 mapping: one thread per (x, y) column and ZPT consecutive slices; the
-// per-(x, y, view) geometry (asin, sqrt, reciprocal) is computed once and
-// amortised over the z-column held in registers (s, h, image per slice).  The
-// per-view trigonometric table is built on the host with the reference's float
-// expressions.  Samples are gathered through the read-only cache.
+// GB300 mapping: one thread per (x, y) column and ZPT (8) consecutive
+// slices, 128-thread CTAs of 32 x 4 columns, each warp an 8 x 4 tile so that
+// its gathers fall on few detector channels.  Per angle i the asin and root
+// of the k = 0 view serve all half turns (p only changes sign), and a
+// warp-uniform window limits k to the half turns whose rays can reach the
+// chunk.  Per visited (i, k) the geometry is computed once for the chunk,
+// which a warp vote classes as flat (W = 1), inner (all |q| < 1) or other
+// (window edge, clamps, last-turn border); slices run in pairs with packed
+// FP32 (FFMA2 / FADD2 / FMUL2); the per-angle sums s, h stay in registers and
+// the image sums in shared memory.  The per-view table (theta, sin, cos and
+// the ray term) is built on the host with the reference's float expressions.
+// Samples are gathered through the read-only cache.
 #include <cuda_runtime.h>
 
 #include <cmath>
