@@ -7,16 +7,20 @@
 // size M = 2 * 2^ceil(log2 N), and what its GPU filter kernel
 // (include/rebin_filter.cuh:369-409) evaluates as a direct sum.
 //
-// GB300 design: FP32 FFT convolution entirely in shared memory.  Two real rows
-// are packed into one complex row (x_a + i x_b); because the kernel is real the
+// GB300 design: FP32 FFT convolution in shared memory.  Two real rows are
+// packed into one complex row (x_a + i x_b); because the kernel is real the
 // real and imaginary parts of the inverse transform are the two filtered rows.
-// Each CTA is persistent, loads the twiddle table once and then loops over row
-// pairs: load (coalesced) -> forward Stockham passes (radix 16 in registers, one
-// radix-2/4/8 pass first when log2 M is not a multiple of 4; three passes for
-// M = 4096) -> multiply by the kernel spectrum H/M (fused into the first
-// inverse pass) -> inverse passes -> store.  Shared-memory indices are padded
-// by one element per 32 so the strided Stockham stores are conflict-free.  HBM traffic is one read and
-// one write of the rows; the transform lives in shared memory.
+// CTAs are persistent and loop over row pairs.  For M = 4096 (row lengths
+// 1025..2048, every built-in scanner) ramp_fft4096_kernel runs 16 x 16 x 16
+// radix-16 passes: thread j owns butterfly j of every pass, the first forward
+// pass reads the rows from HBM (inputs >= M/2 are the zero padding), the last
+// forward pass, the spectrum multiply and the first inverse pass stay in
+// registers, and the last inverse pass writes HBM -- four shared-memory round
+// trips per pair, indices padded by one element per 16 (conflict-free), pass
+// twiddles from [r][k] tables, 16-point DFTs as 4 x 4 with the complex adds as
+// packed FP32.  Other M take ramp_fft_kernel (radix 16 Stockham passes, one
+// radix-2/4/8 pass first when log2 M is not a multiple of 4).  HBM traffic is
+// one read and one write of the rows.
 #include <cuda_runtime.h>
 
 #include <atomic>

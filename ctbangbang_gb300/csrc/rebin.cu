@@ -19,6 +19,10 @@
 // that no multiply-add is fused.  The unfiltered result is therefore bit-exact
 // with the reference CPU path compiled without FMA contraction.
 //
+// A thread covers one output channel, 8 views and 4 raw rows: the view-axis
+// taps of a (channel, view) are computed once for its rows.  A launch may
+// cover a range of views (the streamed whole-scan path).
+//
 // Output layout: rebin[view][out_row][channel_os], views = n_proj/n_ffs -
 // 2*add_projections (the leading add_projections views are dropped, as the
 // reference's copy loops do, e.g. src/rebin_filter_cpu.cu:119-131).
