@@ -1,7 +1,8 @@
-// abi.cu -- the library's C ABI: context, device-resident stages, the
-// whole-scan device path and the drop-in module functions with the reference's
-// semantics (host buffers in, host buffers out, d_rebin handed from rebin_filter
-// to backproject).
+// abi.cu -- the library's C ABI: the work-buffer context (bound to one
+// device), the device stages, the block-loop and whole-scan reconstruction
+// paths (device buffers, host buffers, the raw file) and the drop-in module
+// functions with the reference's semantics (host buffers in, host buffers
+// out, d_rebin handed from rebin_filter to backproject).
 #include <cuda_runtime.h>
 #include <fcntl.h>
 #include <unistd.h>

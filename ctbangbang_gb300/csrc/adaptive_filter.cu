@@ -21,8 +21,11 @@
 // without fused multiply-adds.  GB300 mapping: step 1 is a CTA reduction per
 // frame, steps 2-3 one thread per frame, step 4 one warp per frame (the window
 // counts are integers, so splitting them across lanes is exact), step 5 a
-// per-frame float4 stream that smooths only the samples above the threshold
-// (rows of a multiple of 4 channels; otherwise a shared-memory tiled stencil).
+// per-frame float4 copy that lists the samples above the threshold in shared
+// memory and smooths them after the copy (rows of a multiple of 4 channels;
+// otherwise a shared-memory tiled stencil).  Every step takes a frame range,
+// so a window whose frames arrive in order can be filtered as they come
+// (AfStream).
 #include <cuda_runtime.h>
 
 #include <algorithm>
