@@ -164,6 +164,34 @@ def test_dropin_pipeline_vs_oracle(torch_cuda, oracle_lib, lib, tmp_path, varian
     scan.close()
 
 
+def shape_spec(variant):
+    if variant == "odd_image":  # neither side a multiple of the 32 x 4 CTA or 8 x 4 warp tile
+        return scans.tiny(0, 1, adaptive_filtration=2.0, nx=37, ny=29, seed=61)
+    if variant == "pitch_0.6":  # more half turns in the pull window, two blocks
+        return scans.tiny(1, 1, adaptive_filtration=2.0, pitch=0.6, n_slices=14, slice_thickness=2.5, seed=62)
+    if variant == "pitch_1.4":
+        return scans.tiny(1, 0, adaptive_filtration=2.0, pitch=1.4, seed=63)
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, nx=40, ny=40, seed=64)
+    spec.x_origin, spec.y_origin, spec.tube_start_angle = 7.5, -4.0, 30.0
+    return spec
+
+
+@pytest.mark.parametrize("variant", ["odd_image", "pitch_0.6", "pitch_1.4", "offset_origin"])
+def test_image_shapes_and_helices_vs_oracle(torch_cuda, oracle_lib, lib, tmp_path, variant):
+    """Image sides off the thread tiling, other pitches, an off-centre field
+    of view with a rotated tube start: the drop-in block loop against the
+    oracle, end to end."""
+    scan = H.Scan(shape_spec(variant), str(tmp_path))
+    img_g, fin_g = run_dropin(scan)
+    reset_blocks(scan)
+    scan.mr.ctd.final_image_stack = None  # the drop-in's stack stays allocated (test only)
+    img_o, fin_o = run_oracle(oracle_lib, scan)
+    assert float(np.abs(img_o).max()) > 0.01
+    assert_hu(img_g, img_o)
+    assert_hu(fin_g, fin_o)
+    scan.close()
+
+
 def test_reconstruct_device_equals_dropin(torch_cuda, lib, tmp_path):
     torch = torch_cuda
     spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=41)
