@@ -254,6 +254,39 @@ extern "C" int ctbb_configure_recon_params(const char *prm_path, struct recon_pa
         set_error("%s was not properly set in configuration", missing);
         return CTBB_ERR_CONFIG;
     }
+    // Values the reference takes as they come and that would only fail later
+    // (or not at all) in planning and reconstruction: rejected here.
+    const struct {
+        const char *name;
+        float v;
+        bool positive;
+    } floats[] = {
+        {"CollSlicewidth", rp.coll_slicewidth, true}, {"SliceThickness", rp.slice_thickness, true},
+        {"AcqFOV", rp.acq_fov, true},                  {"ReconFOV", rp.recon_fov, true},
+        {"PitchValue", rp.pitch_value, false},         {"StartPos", rp.start_pos, false},
+        {"EndPos", rp.end_pos, false},                 {"Xorigin", rp.x_origin, false},
+        {"Yorigin", rp.y_origin, false},               {"TubeStartAngle", rp.tube_start_angle, false},
+        {"AdaptiveFiltration", rp.adaptive_filtration_s, false},
+    };
+    for (const auto &f : floats) {
+        if (!std::isfinite(f.v) || (f.positive && !(f.v > 0.0f))) {
+            set_error("%s: %g is not a %snumber", f.name, (double)f.v, f.positive ? "positive finite " : "finite ");
+            return CTBB_ERR_CONFIG;
+        }
+    }
+    const unsigned kMaxSide = 16384;
+    if (rp.nx > kMaxSide || rp.ny > kMaxSide) {
+        set_error("Nx/Ny %u x %u: each side must be 1..%u", rp.nx, rp.ny, kMaxSide);
+        return CTBB_ERR_CONFIG;
+    }
+    if (rp.n_rows < 0 || rp.n_readings < 0 || rp.n_slices < 0) {
+        set_error("Nrows %d, Readings %d, NSlices %d: negative", rp.n_rows, rp.n_readings, rp.n_slices);
+        return CTBB_ERR_CONFIG;
+    }
+    if ((rp.z_ffs != 0 && rp.z_ffs != 1) || (rp.phi_ffs != 0 && rp.phi_ffs != 1)) {
+        set_error("Zffs %d / Phiffs %d: each must be 0 or 1", rp.z_ffs, rp.phi_ffs);
+        return CTBB_ERR_CONFIG;
+    }
     return CTBB_OK;
 }
 

@@ -125,6 +125,34 @@ def test_prm_missing_key_is_an_error_not_exit(lib, tmp_path):
     assert rp.n_rows == 16
 
 
+@pytest.mark.parametrize("key,value", [
+    ("SliceThickness:", "-2.0"), ("CollSlicewidth:", "inf"), ("PitchValue:", "nan"), ("ReconFOV:", "-1"),
+    ("Xorigin:", "nan"), ("Nx:", "-512"), ("Ny:", "100000"), ("Zffs:", "2"), ("Readings:", "-5"),
+])
+def test_prm_out_of_range_values_are_config_errors(lib, tmp_path, key, value):
+    """Values the reference would carry into planning (negative or non-finite
+    sizes, a negative side parsed as a huge unsigned, FFS flags other than 0/1)
+    are rejected by the parser with a status, never by exit() or a crash."""
+    prm, _ = scans.prepare(scans.tiny(0, 0), str(tmp_path))
+    txt = open(prm).read()
+    assert re.search(r"^%s\s" % re.escape(key), txt, flags=re.M), key
+    open(prm, "w").write(re.sub(r"^%s\s.*$" % re.escape(key), "%s\t%s" % (key, value), txt, flags=re.M))
+    rp = structs.ReconParams()
+    st = lib.ctbb_configure_recon_params(prm.encode(), C.byref(rp))
+    assert L.STATUS[st] == "CTBB_ERR_CONFIG", (key, value, lib.ctbb_last_error())
+    assert key[:-1].encode() in lib.ctbb_last_error() or b"Nx/Ny" in lib.ctbb_last_error()
+
+
+def test_missing_raw_file_is_an_io_error(lib, tmp_path):
+    spec = scans.tiny(0, 0)
+    mr = scans.plan_spec(spec, str(tmp_path))
+    mr.rp.raw_data_file = b"not_there.raw"
+    L.call("ctbb_update_block_info", C.byref(mr))
+    st = lib.ctbb_extract_projections(C.byref(mr))
+    assert L.STATUS[st] == "CTBB_ERR_IO", lib.ctbb_last_error()
+    scans.free_plan(mr)
+
+
 def test_prm_parser_matches_reference(lib, ref_lib, tmp_path):
     spec = scans.CONFIGS["config2"]
     prm, _ = scans.prepare(spec, str(tmp_path))
