@@ -46,6 +46,7 @@ PROTOTYPES = {
     "ctbb_rebin_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_ramp_filter_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),
+    "ctbb_write_dicom_series": (C.c_int, [_MR, _F, C.c_int, C.c_float, C.c_char_p]),
     "ctbb_finalize_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
     "ctbb_reconstruct_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
     "ctbb_reconstruct_scan_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),

@@ -238,6 +238,19 @@ int ctbb_extract_projections(struct recon_metadata *mr);
    src/setup.cu:769-787. */
 int ctbb_finish_and_cleanup(struct recon_metadata *mr);
 
+/* The final stack h_stack [n_slices][ny][nx] (host) as a DICOM CT image
+   series, one file per slice, <out_dir>/<OutputFile stem>_<k+1, 4 digits>.dcm
+   ("slice" when OutputFile is empty).  No counterpart in the reference, which
+   writes the raw float32 stack (finish_and_cleanup, src/setup.cu:769-787).
+   mu_water > 0: the stack holds attenuation (1/mm) and is written as
+   1000 (mu - mu_water) / mu_water; mu_water = 0: it already holds HU.  Pixels
+   are int16 HU (rounded, clamped), rescale slope 1, intercept 0; explicit VR
+   little endian; pixel (i, j) at the backprojector's voxel centre, slice k at
+   StartPos + dir k SliceThickness; fresh 2.25 study / series UIDs per call.
+   No patient identity is written (PatientName and PatientID empty). */
+int ctbb_write_dicom_series(const struct recon_metadata *mr, const float *h_stack,
+                            int n_slices, float mu_water, const char *out_dir);
+
 /* Number of final slices: floor(|end-start|/slice_thickness)+1
    (src/finalize_image_stack_cpu.cu:67). */
 int ctbb_n_slices_final(const struct recon_metadata *mr);
