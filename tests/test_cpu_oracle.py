@@ -89,7 +89,10 @@ def test_oracle_matches_reference_golden(lib, oracle_lib, tmp_path, path):
         if SAME_LIBM_AS_GOLDEN:
             np.testing.assert_array_equal(got_f, z["filtered_b%d" % b])
         else:
-            np.testing.assert_allclose(got_f, z["filtered_b%d" % b], rtol=0, atol=2e-6 * np.abs(got_f).max())
+            # the ramp filter (a high-pass: outputs far below its inputs) carries
+            # the rebin's ulp-level input differences; 3.4e-6 of the row
+            # maximum seen on aarch64
+            np.testing.assert_allclose(got_f, z["filtered_b%d" % b], rtol=0, atol=1e-5 * np.abs(got_f).max())
     if SAME_LIBM_AS_GOLDEN:
         np.testing.assert_array_equal(H.view(mr.ctd.image, d["n_image"]), z["image"])
     else:
