@@ -50,6 +50,7 @@ namespace {
 
 struct BpParams {
     const float *rebin;    // [V][R][Nos]
+    uint64_t rebin_rows;   // address of rebin - kFloorMagicBits rows (mod 2^64): see row_floor
     float *out;            // [n_slices_block][ny][nx]
     const float4 *views;   // [n_half][nht] {theta, sin, cos, theta z_rot / 2 pi'}
     const float *zpos;     // [n_slices_block]
@@ -126,12 +127,28 @@ __device__ __forceinline__ float asin_fast(float a)
     return fmaf(a * t, p, a);
 }
 
+// Row floors through the float unit: for |ql| < 2^22, ql + 1.5 2^23 rounded
+// down is exactly 1.5 2^23 + floor(ql) (the binade [2^23, 2^24) has unit
+// spacing), so one packed add gives both the floor as a float (t - 1.5 2^23,
+// exact) and as an integer (the bits of t are kFloorMagicBits + floor(ql)).
+// The row address is then view + bits(t) * row stride with the view's base
+// moved back by kFloorMagicBits rows (64-bit modular arithmetic, folded into
+// BpParams::rebin_rows on the host): one multiply-add, no conversion.
+constexpr float kFloorMagic = 12582912.0f;       // 1.5 * 2^23
+constexpr uint32_t kFloorMagicBits = 0x4B400000u;  // its bits
+__device__ __forceinline__ float2 row_floor(float2 ql)
+{
+    return __fadd2_rd(ql, make_float2(kFloorMagic, kFloorMagic));
+}
+
 // The 2x2 footprint {(p, row), (p+1, row), (p, row+1), (p+1, row+1)} of a
-// view, row in [0, R-2]; `view` points at (p, 0).
-__device__ __forceinline__ void fetch_footprint(const float *view, int nos, float row, float &v00, float &v01,
+// view, row in [0, R-2] given as t = kFloorMagic + row (row_floor);
+// `view_rows` is the view's (p, 0) address moved back by kFloorMagicBits rows.
+__device__ __forceinline__ void fetch_footprint(uint64_t view_rows, int nos, float t, float &v00, float &v01,
                                                 float &v10, float &v11)
 {
-    const float *r0 = view + (int)row * nos;
+    const float *r0 = reinterpret_cast<const float *>(
+        view_rows + (uint64_t)__float_as_uint(t) * (uint64_t)((unsigned)nos * sizeof(float)));
     v00 = __ldg(r0);
     v01 = __ldg(r0 + 1);
     v10 = __ldg(r0 + nos);
@@ -244,7 +261,8 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             bool last = (k == p.nht - 1);
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
-            const float *view = p.rebin + (size_t)(unsigned)(i + k * p.n_half) * view_stride + ip;
+            const uint64_t view_rows =
+                p.rebin_rows + ((uint64_t)(unsigned)(i + k * p.n_half) * view_stride + (unsigned)ip) * sizeof(float);
             // Slices are processed in pairs (z, z + 1) with packed FP32
             // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
             // conversions and loads stay per slice.
@@ -252,12 +270,13 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             const float2 omwp2 = make_float2(1.0f - wp, 1.0f - wp);
             const float2 dq2 = make_float2(dq, dq), q02 = make_float2(q0, q0);
             const float2 hr2 = make_float2(p.half_rows, p.half_rows);
-            // bilinear value of a pair from its rows (clamped or not by the caller)
-            auto pair_value = [&](float2 ql, float2 row) -> float2 {
-                float2 wq = sub2(ql, row);
+            // bilinear value of a pair from its rows t = kFloorMagic + row
+            // (clamped or not by the caller)
+            auto pair_value = [&](float2 ql, float2 tr) -> float2 {
+                float2 wq = sub2(ql, sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
                 float a00, a01, a10, a11, b00, b01, b10, b11;
-                fetch_footprint(view, nos, row.x, a00, a01, a10, a11);
-                fetch_footprint(view, nos, row.y, b00, b01, b10, b11);
+                fetch_footprint(view_rows, nos, tr.x, a00, a01, a10, a11);
+                fetch_footprint(view_rows, nos, tr.y, b00, b01, b10, b11);
                 float2 c0 = fma2(wp2, make_float2(a01, b01), mul2(omwp2, make_float2(a00, b00)));
                 float2 c1 = fma2(wp2, make_float2(a11, b11), mul2(omwp2, make_float2(a10, b10)));
                 return fma2(wq, sub2(c1, c0), c0);
@@ -295,8 +314,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                         for (int mm = 0; mm < SUB / 2; ++mm) {
                             const int m = sc * (SUB / 2) + mm;
                             float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
-                            float2 row = make_float2(floorf(ql.x), floorf(ql.y));
-                            s2[m] = add2(s2[m], pair_value(ql, row));
+                            s2[m] = add2(s2[m], pair_value(ql, row_floor(ql)));
                         }
                     }
                     ++n_flat[sc];
@@ -312,8 +330,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                             float2 w = pair_weight(q);
                             h2[m] = add2(h2[m], w);
                             float2 ql = fma2(q, hr2, hr2);
-                            float2 row = make_float2(floorf(ql.x), floorf(ql.y));
-                            s2[m] = fma2(w, pair_value(ql, row), s2[m]);
+                            s2[m] = fma2(w, pair_value(ql, row_floor(ql)), s2[m]);
                         }
                     } else {
 #pragma unroll
@@ -330,7 +347,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                 // when p is off the detector) and validity only scales the weight, so
                 // the loads of all slices can be issued together.  Only a warp with
                 // a row near the last-turn border takes the per-slice border test.
-                const float row_max = (float)(p.n_rows - 2);
+                const float t_max = kFloorMagic + (float)(p.n_rows - 2);  // row R-2
                 bool border = last && fmaf(q_endc, p.half_rows, p.half_rows) > q_max_last - kBorderBand;
                 if (__any_sync(lanes, border)) {
 #pragma unroll
@@ -342,9 +359,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                         w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
                         h2[m] = add2(h2[m], w);
                         float2 ql = fma2(q, hr2, hr2);
-                        float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
-                                                 fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
-                        float2 v = pair_value(ql, row);
+                        float2 tr = row_floor(ql);
+                        tr = make_float2(fminf(fmaxf(tr.x, kFloorMagic), t_max), fminf(fmaxf(tr.y, kFloorMagic), t_max));
+                        float2 v = pair_value(ql, tr);
                         bool ok_x = p_ok && in_x, ok_y = p_ok && in_y;
                         if (ok_x) {
                             float d = ql.x - q_max_last;
@@ -374,9 +391,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                     w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
                     h2[m] = add2(h2[m], w);
                     float2 ql = fma2(q, hr2, hr2);
-                    float2 row = make_float2(fminf(fmaxf(floorf(ql.x), 0.0f), row_max),
-                                             fminf(fmaxf(floorf(ql.y), 0.0f), row_max));
-                    float2 v = pair_value(ql, row);
+                    float2 tr = row_floor(ql);
+                    tr = make_float2(fminf(fmaxf(tr.x, kFloorMagic), t_max), fminf(fmaxf(tr.y, kFloorMagic), t_max));
+                    float2 v = pair_value(ql, tr);
                     s2[m] = fma2(p_ok ? w : make_float2(0.0f, 0.0f), v, s2[m]);
                 }
             }
@@ -490,6 +507,10 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     const float pi = kPiBackproject;
     BpParams p;
     p.rebin = d_rebin;
+    // row_floor's addressing: the base moved back by kFloorMagicBits rows,
+    // modulo 2^64 (every row address comes back inside the buffer)
+    p.rebin_rows = (uint64_t)(uintptr_t)d_rebin -
+                   (uint64_t)kFloorMagicBits * (uint64_t)cg.n_channels_oversampled * sizeof(float);
     p.out = d_block;
     p.views = d_views;
     p.zpos = d_zpos;
