@@ -20,7 +20,7 @@ CUDA_SOURCES = [
     "abi.cu", "adaptive_filter.cu", "rebin.cu", "ramp_filter.cu",
     "backproject.cu", "finalize.cu", "phantom.cu", "peak_probe.cu",
 ]
-HOST_SOURCES = ["planner.cpp", "dicom.cpp"]
+HOST_SOURCES = ["planner.cpp", "dicom.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

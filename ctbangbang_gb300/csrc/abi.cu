@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <new>
 #include <condition_variable>
 #include <mutex>
 #include <string>
@@ -200,7 +201,7 @@ int num_sms()
 
 void count_launch(uint64_t n) { ctx().launches += n; }
 
-int require_device()
+int require_device(Context &c)
 {
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
@@ -213,7 +214,6 @@ int require_device()
     // call; another device must not reach them
     int dev = 0;
     CTBB_CUDA_TRY(cudaGetDevice(&dev));
-    Context &c = ctx();
     int bound = -1;
     if (!c.device.compare_exchange_strong(bound, dev) && bound != dev) {
         set_error("the library's work buffers live on device %d, the current device is %d: call "
@@ -223,20 +223,21 @@ int require_device()
     return CTBB_OK;
 }
 
+// the library-wide context's device (the no-allocation path, the peak probe)
+int require_device() { return require_device(ctx()); }
+
 // ---- stage implementations (device pointers, stream-ordered) --------------
 
-static int do_adaptive(const struct recon_metadata &mr, const float *d_in, float *d_out)
+static int do_adaptive(Context &c, const struct recon_metadata &mr, const float *d_in, float *d_out)
 {
-    Context &c = ctx();
     size_t n = adaptive_filter_scratch_floats(mr.ri.n_proj_pull);
     CTBB_TRY(c.scratch.ensure(n * sizeof(float)));
     StageScope scope(c, 0);
     return launch_adaptive_filter(mr, d_in, d_out, c.scratch.as<float>(), c.stream);
 }
 
-static int do_rebin(const struct recon_metadata &mr, const float *d_raw, float *d_rebin)
+static int do_rebin(Context &c, const struct recon_metadata &mr, const float *d_raw, float *d_rebin)
 {
-    Context &c = ctx();
     RebinTables t;
     CTBB_TRY(build_rebin_tables(mr, &t));
     CTBB_TRY(upload_rebin_tables(t, &c.rebin_tables, c.stream));
@@ -244,9 +245,8 @@ static int do_rebin(const struct recon_metadata &mr, const float *d_raw, float *
     return launch_rebin(t, c.rebin_tables, d_raw, d_rebin, c.stream);
 }
 
-static int do_filter(const struct recon_metadata &mr, float *d_rebin)
+static int do_filter(Context &c, const struct recon_metadata &mr, float *d_rebin)
 {
-    Context &c = ctx();
     BlockDims d = block_dims(mr);
     std::vector<float> taps(2 * d.n_os);
     CTBB_TRY(ctbb_load_filter(&mr, taps.data()));
@@ -255,9 +255,8 @@ static int do_filter(const struct recon_metadata &mr, float *d_rebin)
     return launch_ramp_filter(c.ramp, d_rebin, d.n_views * d.n_rows, c.stream);
 }
 
-static int do_backproject(const struct recon_metadata &mr, const float *d_rebin, float *d_block)
+static int do_backproject(Context &c, const struct recon_metadata &mr, const float *d_rebin, float *d_block)
 {
-    Context &c = ctx();
     BackprojectTables t;
     CTBB_TRY(build_backproject_tables(mr, &t));
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
@@ -267,9 +266,8 @@ static int do_backproject(const struct recon_metadata &mr, const float *d_rebin,
                               bp_zpt(), c.stream);
 }
 
-static int do_finalize(const struct recon_metadata &mr, const float *d_image, float *d_final, float mu_water)
+static int do_finalize(Context &c, const struct recon_metadata &mr, const float *d_image, float *d_final, float mu_water)
 {
-    Context &c = ctx();
     FinalizeTables t;
     CTBB_TRY(build_finalize_tables(mr, &t));
     CTBB_TRY(upload(c.fin_offsets, t.offsets, c.stream));
@@ -298,15 +296,23 @@ extern "C" int ctbb_set_stream(void *stream)
 
 extern "C" uint64_t ctbb_kernel_launch_count(void) { return ctx().launches.load(); }
 
-extern "C" int ctbb_release_workspace(void)
+// Frees every work buffer, table, copy stream and staging buffer of c, on the
+// device they live on.  device_sync: wait for the whole device first (the
+// default context, whose stream the caller chooses); else for c's streams.
+// unbind: forget the device, so that the next call may use another one.
+static void release_context(Context &c, bool device_sync, bool unbind)
 {
-    Context &c = ctx();
-    std::lock_guard<std::mutex> lk(c.mu);
-    // release on the device the buffers belong to
     int cur = 0, bound = c.device.load();
     cudaGetDevice(&cur);
     if (bound >= 0 && bound != cur) cudaSetDevice(bound);
-    if (bound >= 0) cudaDeviceSynchronize();
+    if (bound >= 0) {
+        if (device_sync) {
+            cudaDeviceSynchronize();
+        } else {
+            cudaStreamSynchronize(c.stream);
+            if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+        }
+    }
     for (DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                             &c.scratch, &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices, &c.fin_weights})
         b->release();
@@ -332,9 +338,18 @@ extern "C" int ctbb_release_workspace(void)
         cudaStreamDestroy(c.copy_stream);
         c.copy_stream = nullptr;
     }
-    c.sms = 0;
-    c.device.store(-1);
+    if (unbind) {
+        c.sms = 0;
+        c.device.store(-1);
+    }
     if (bound >= 0 && bound != cur) cudaSetDevice(cur);
+}
+
+extern "C" int ctbb_release_workspace(void)
+{
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    release_context(c, true, true);
     return CTBB_OK;
 }
 
@@ -363,18 +378,20 @@ extern "C" int ctbb_adaptive_filter_device(const struct recon_metadata *mr, cons
 {
     clear_error();
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    std::lock_guard<std::mutex> lk(ctx().mu);
-    return do_adaptive(*mr, d_in, d_out);
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return do_adaptive(c, *mr, d_in, d_out);
 }
 
 extern "C" int ctbb_rebin_device(const struct recon_metadata *mr, const float *d_raw, float *d_rebin)
 {
     clear_error();
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    std::lock_guard<std::mutex> lk(ctx().mu);
-    return do_rebin(*mr, d_raw, d_rebin);
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return do_rebin(c, *mr, d_raw, d_rebin);
 }
 
 extern "C" int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os, const float *h_taps)
@@ -384,7 +401,7 @@ extern "C" int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os,
         set_error("ctbb_ramp_filter_device: bad argument");
         return CTBB_ERR_ARGUMENT;
     }
-    CTBB_TRY(require_device());
+    CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     CTBB_TRY(prepare_ramp_filter(h_taps, n_os, &c.ramp, c.stream));
@@ -395,9 +412,10 @@ extern "C" int ctbb_backproject_device(const struct recon_metadata *mr, const fl
 {
     clear_error();
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    std::lock_guard<std::mutex> lk(ctx().mu);
-    return do_backproject(*mr, d_rebin, d_block);
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return do_backproject(c, *mr, d_rebin, d_block);
 }
 
 extern "C" int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image, float *d_final,
@@ -405,9 +423,10 @@ extern "C" int ctbb_finalize_device(const struct recon_metadata *mr, const float
 {
     clear_error();
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    std::lock_guard<std::mutex> lk(ctx().mu);
-    return do_finalize(*mr, d_image, d_final, mu_water);
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return do_finalize(c, *mr, d_image, d_final, mu_water);
 }
 
 extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
@@ -423,7 +442,7 @@ extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
     return 2 * raw + rebin + image;
 }
 
-extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+static int reconstruct_device_in(Context &c, struct recon_metadata *mr, const float *d_scan, float *d_final,
                                        float mu_water)
 {
     clear_error();
@@ -432,8 +451,7 @@ extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d
         return CTBB_ERR_ARGUMENT;
     }
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
+    CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const size_t n_readings = (size_t)mr->rp.n_readings;
@@ -464,16 +482,22 @@ extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d
             d_win = c.raw_in.as<float>();
         }
         CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
-        CTBB_TRY(do_adaptive(*mr, d_win, c.raw_filt.as<float>()));
+        CTBB_TRY(do_adaptive(c, *mr, d_win, c.raw_filt.as<float>()));
         CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
-        CTBB_TRY(do_rebin(*mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
-        CTBB_TRY(do_filter(*mr, c.rebin.as<float>()));
+        CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+        CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
         float *slab = c.image.as<float>() + b * n_block * plane;
-        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>(), slab));
+        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab));
     }
-    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), d_final, mu_water));
+    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
+}
+
+extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+                                       float mu_water)
+{
+    return reconstruct_device_in(ctx(), mr, d_scan, d_final, mu_water);
 }
 
 // Every block's plan, as the block loop makes them, and the union of their
@@ -511,6 +535,26 @@ static int plan_union(struct recon_metadata *mr, std::vector<struct recon_info> 
     return CTBB_OK;
 }
 
+// Device bytes the whole-scan paths (scan_device / scan_host / scan_file)
+// hold for this plan: the union window raw and filtered, its rebinned rows,
+// the adaptive filter's statistics, the image and final stacks, plus 8 MiB
+// for tables and staging slack.  0 if the plan is not usable.
+extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
+{
+    if (!mr || check_mr(mr) || !mr->table_positions) return 0;
+    struct recon_metadata m = *mr;  // plan_union advances the block index
+    std::vector<struct recon_info> blocks;
+    long long g0 = 0, g1 = 0;
+    struct recon_metadata mg;
+    if (plan_union(&m, &blocks, &g0, &g1, &mg) != CTBB_OK) return 0;
+    BlockDims dg = block_dims(mg);
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    const int n_final = ctbb_n_slices_final(mr);
+    return (2 * dg.raw_elems() + dg.rebin_elems() + adaptive_filter_scratch_floats(dg.n_proj_pull) +
+            plane * mr->ri.n_slices_recon + plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
+           ((size_t)8 << 20);
+}
+
 // first rebinned view of block b in the union's rebinned rows
 static size_t union_view_offset(const struct recon_info &ri, long long g0)
 {
@@ -524,7 +568,7 @@ static size_t union_view_offset(const struct recon_info &ri, long long g0)
 // again for every block).  Differs from the block loop only in the adaptive
 // filter's 18- and 180-degree statistics windows, which here are not cut at
 // the edges of each block's window.
-extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, const float *d_scan, float *d_final,
                                             float mu_water)
 {
     clear_error();
@@ -533,8 +577,7 @@ extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const flo
         return CTBB_ERR_ARGUMENT;
     }
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
+    CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const long long n_readings = (long long)mr->rp.n_readings;
@@ -560,21 +603,27 @@ extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const flo
     }
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    CTBB_TRY(do_adaptive(mg, d_win, c.raw_filt.as<float>()));
+    CTBB_TRY(do_adaptive(c, mg, d_win, c.raw_filt.as<float>()));
     CTBB_TRY(c.rebin.ensure(dg.rebin_elems() * sizeof(float)));
-    CTBB_TRY(do_rebin(mg, c.raw_filt.as<float>(), c.rebin.as<float>()));
-    CTBB_TRY(do_filter(mg, c.rebin.as<float>()));
+    CTBB_TRY(do_rebin(c, mg, c.raw_filt.as<float>(), c.rebin.as<float>()));
+    CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
     const size_t view_elems = dg.n_rows * dg.n_os;
     for (size_t b = 0; b < blocks.size(); ++b) {
         mr->ri = blocks[b];
         // view j of block b is view j + (pull_start_b - g0) / n_ffs of the union
         size_t off = union_view_offset(blocks[b], g0);
         float *slab = c.image.as<float>() + b * n_block * plane;
-        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>() + off * view_elems, slab));
+        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>() + off * view_elems, slab));
     }
-    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), d_final, mu_water));
+    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
+}
+
+extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
+                                            float mu_water)
+{
+    return reconstruct_scan_device_in(ctx(), mr, d_scan, d_final, mu_water);
 }
 
 // --------------------------------------------------------------------------
@@ -589,7 +638,7 @@ extern "C" int ctbb_adaptive_filter_kk(struct recon_metadata *mr)
         set_error("adaptive_filter_kk: ctd.raw is null");
         return CTBB_ERR_STATE;
     }
-    CTBB_TRY(require_device());
+    CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     BlockDims d = block_dims(*mr);
@@ -597,7 +646,7 @@ extern "C" int ctbb_adaptive_filter_kk(struct recon_metadata *mr)
     CTBB_TRY(c.raw_in.ensure(bytes));
     CTBB_TRY(c.raw_filt.ensure(bytes));
     CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.ptr, mr->ctd.raw, bytes, cudaMemcpyHostToDevice, c.stream));
-    CTBB_TRY(do_adaptive(*mr, c.raw_in.as<float>(), c.raw_filt.as<float>()));
+    CTBB_TRY(do_adaptive(c, *mr, c.raw_in.as<float>(), c.raw_filt.as<float>()));
     CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.raw, c.raw_filt.ptr, bytes, cudaMemcpyDeviceToHost, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
@@ -611,7 +660,7 @@ extern "C" int ctbb_rebin_filter(struct recon_metadata *mr)
         set_error("rebin_filter: ctd.raw is null");
         return CTBB_ERR_STATE;
     }
-    CTBB_TRY(require_device());
+    CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     BlockDims d = block_dims(*mr);
@@ -627,8 +676,8 @@ extern "C" int ctbb_rebin_filter(struct recon_metadata *mr)
     CTBB_CUDA_TRY(cudaMalloc(&d_rebin, rebin_bytes));
     mr->ctd.d_rebin = d_rebin;
     c.our_d_rebin = d_rebin;
-    CTBB_TRY(do_rebin(*mr, c.raw_in.as<float>(), d_rebin));
-    CTBB_TRY(do_filter(*mr, d_rebin));
+    CTBB_TRY(do_rebin(c, *mr, c.raw_in.as<float>(), d_rebin));
+    CTBB_TRY(do_filter(c, *mr, d_rebin));
     if (mr->flags.testing && mr->ctd.rebin)
         CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.rebin, d_rebin, rebin_bytes, cudaMemcpyDeviceToHost, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
@@ -647,13 +696,13 @@ extern "C" int ctbb_backproject(struct recon_metadata *mr)
         set_error("backproject: block_idx %d outside 1..%zu", mr->ri.cb.block_idx, mr->ri.n_blocks);
         return CTBB_ERR_STATE;
     }
-    CTBB_TRY(require_device());
+    CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     size_t block_elems = plane * mr->ri.n_slices_block;
     CTBB_TRY(c.block.ensure(block_elems * sizeof(float)));
-    CTBB_TRY(do_backproject(*mr, mr->ctd.d_rebin, c.block.as<float>()));
+    CTBB_TRY(do_backproject(c, *mr, mr->ctd.d_rebin, c.block.as<float>()));
     size_t block_offset = (size_t)(mr->ri.cb.block_idx - 1) * block_elems;
     CTBB_CUDA_TRY(cudaMemcpyAsync(mr->ctd.image + block_offset, c.block.ptr, block_elems * sizeof(float),
                                   cudaMemcpyDeviceToHost, c.stream));
@@ -672,7 +721,7 @@ static int finalize_common(struct recon_metadata *mr, float mu_water)
         set_error("finalize_image_stack: ctd.image is null");
         return CTBB_ERR_STATE;
     }
-    CTBB_TRY(require_device());
+    CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
@@ -682,7 +731,7 @@ static int finalize_common(struct recon_metadata *mr, float mu_water)
     CTBB_TRY(c.image.ensure(n_img * sizeof(float)));
     CTBB_TRY(c.final_stack.ensure(n_out * sizeof(float)));
     CTBB_CUDA_TRY(cudaMemcpyAsync(c.image.ptr, mr->ctd.image, n_img * sizeof(float), cudaMemcpyHostToDevice, c.stream));
-    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
     float *host = (float *)calloc(n_out ? n_out : 1, sizeof(float));
     if (!host) {
         set_error("finalize_image_stack: host allocation failed");
@@ -868,7 +917,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             if (need > (size_t)v_done && v_done < V) break;
             mr->ri = blocks[b_done];
             float *slab = c.image.as<float>() + b_done * n_block * plane;
-            status = do_backproject(*mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
+            status = do_backproject(c, *mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
                                     slab);
             ++b_done;
         }
@@ -880,7 +929,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
         set_error("whole scan: %zu of %zu blocks left unfinished", blocks.size() - b_done, blocks.size());
         return CTBB_ERR_STATE;
     }
-    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
     CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
                                   cudaMemcpyDeviceToHost, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
@@ -891,7 +940,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
 // chunks on the copy stream while the compute stream works on the chunks
 // that have arrived (scan_streamed).  Same result as
 // ctbb_reconstruct_scan_device.
-extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+static int reconstruct_scan_host_in(Context &c, struct recon_metadata *mr, const float *h_scan, float *h_final,
                                           float mu_water)
 {
     clear_error();
@@ -900,11 +949,16 @@ extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float
         return CTBB_ERR_ARGUMENT;
     }
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
+    CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     HostFeed feed(h_scan, (long long)mr->rp.n_readings, mr->cg.n_rows_raw * mr->cg.n_channels);
     return scan_streamed(c, mr, feed, h_final, mu_water);
+}
+
+extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                                          float mu_water)
+{
+    return reconstruct_scan_host_in(ctx(), mr, h_scan, h_final, mu_water);
 }
 
 // Frames [a, e) of the scan read from a FileType 0 raw file -- frame i at
@@ -1045,7 +1099,7 @@ struct FileFeed : ChunkFeed {
 // Whole scan straight from the raw file (FileType 0): the file is read in
 // chunks while earlier chunks are copied and processed (scan_streamed).
 // Same result as ctbb_reconstruct_scan_device on the file's frames.
-extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float mu_water)
+static int reconstruct_scan_file_in(Context &c, struct recon_metadata *mr, float *h_final, float mu_water)
 {
     clear_error();
     if (!mr || !h_final || !mr->table_positions) {
@@ -1058,8 +1112,7 @@ extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_fi
         return CTBB_ERR_CONFIG;
     }
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
+    CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     char path[4096 + 255 + 2];
     snprintf(path, sizeof(path), "%s/%s", mr->rp.raw_data_dir, mr->rp.raw_data_file);
@@ -1067,7 +1120,12 @@ extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_fi
     return scan_streamed(c, mr, feed, h_final, mu_water);
 }
 
-extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float mu_water)
+{
+    return reconstruct_scan_file_in(ctx(), mr, h_final, mu_water);
+}
+
+static int reconstruct_host_in(Context &c, struct recon_metadata *mr, const float *h_scan, float *h_final,
                                      float mu_water)
 {
     clear_error();
@@ -1076,8 +1134,7 @@ extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_s
         return CTBB_ERR_ARGUMENT;
     }
     CTBB_TRY(check_mr(mr));
-    CTBB_TRY(require_device());
-    Context &c = ctx();
+    CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     CTBB_TRY(ensure_copy_stream(c));
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
@@ -1115,18 +1172,24 @@ extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_s
         CTBB_CUDA_TRY(cudaEventRecord(c.copied[slot], c.copy_stream));
         CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copied[slot], 0));
         CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
-        CTBB_TRY(do_adaptive(*mr, dst, c.raw_filt.as<float>()));
+        CTBB_TRY(do_adaptive(c, *mr, dst, c.raw_filt.as<float>()));
         CTBB_CUDA_TRY(cudaEventRecord(c.consumed[slot], c.stream));
         CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
-        CTBB_TRY(do_rebin(*mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
-        CTBB_TRY(do_filter(*mr, c.rebin.as<float>()));
-        CTBB_TRY(do_backproject(*mr, c.rebin.as<float>(), c.image.as<float>() + b * n_block * plane));
+        CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+        CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
+        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), c.image.as<float>() + b * n_block * plane));
     }
-    CTBB_TRY(do_finalize(*mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
     CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
                                   cudaMemcpyDeviceToHost, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
+}
+
+extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
+                                     float mu_water)
+{
+    return reconstruct_host_in(ctx(), mr, h_scan, h_final, mu_water);
 }
 
 // --------------------------------------------------------------------------
@@ -1168,4 +1231,140 @@ extern "C" int ctbb_profile_read(double *ms, uint64_t *launches, int n, int rese
             c.stage_launches[s] = 0;
         }
     return kProfileStages;
+}
+
+// --------------------------------------------------------------------------
+// contexts: independent work buffers and streams for concurrent scans
+// --------------------------------------------------------------------------
+
+struct ctbb_context_s {
+    Context c;
+    bool own_stream = false;
+};
+
+static size_t context_device_bytes(const Context &c)
+{
+    size_t n = 0;
+    for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
+                                  &c.scratch, &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
+                                  &c.fin_weights})
+        n += b->bytes;
+    return n + c.ramp.capacity * sizeof(float2);
+}
+
+extern "C" int ctbb_context_create(ctbb_context *out)
+{
+    clear_error();
+    if (!out) {
+        set_error("ctbb_context_create: null argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    *out = nullptr;
+    ctbb_context h = new (std::nothrow) ctbb_context_s;
+    if (!h) {
+        set_error("ctbb_context_create: out of host memory");
+        return CTBB_ERR_ALLOC;
+    }
+    int st = require_device(h->c);
+    if (st == CTBB_OK && cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("ctbb_context_create: cudaStreamCreateWithFlags failed");
+        st = CTBB_ERR_CUDA;
+    }
+    if (st != CTBB_OK) {
+        delete h;
+        return st;
+    }
+    h->own_stream = true;
+    *out = h;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_context_destroy(ctbb_context h)
+{
+    clear_error();
+    if (!h) return CTBB_OK;
+    {
+        std::lock_guard<std::mutex> lk(h->c.mu);
+        release_context(h->c, false, false);
+        if (h->own_stream && h->c.stream) cudaStreamDestroy(h->c.stream);
+        h->c.stream = nullptr;
+        for (cudaEvent_t e : h->c.event_pool) cudaEventDestroy(e);
+        h->c.event_pool.clear();
+    }
+    delete h;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_context_set_stream(ctbb_context h, void *stream)
+{
+    clear_error();
+    if (!h) {
+        set_error("ctbb_context_set_stream: null context");
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    cudaStreamSynchronize(h->c.stream);
+    if (h->own_stream && h->c.stream) cudaStreamDestroy(h->c.stream);
+    h->own_stream = false;
+    h->c.stream = reinterpret_cast<cudaStream_t>(stream);
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_context_release_workspace(ctbb_context h)
+{
+    clear_error();
+    if (!h) {
+        set_error("ctbb_context_release_workspace: null context");
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    release_context(h->c, false, false);
+    return CTBB_OK;
+}
+
+extern "C" size_t ctbb_context_device_bytes(ctbb_context h)
+{
+    if (!h) return 0;
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    return context_device_bytes(h->c);
+}
+
+#define CTBB_CONTEXT_CALL(h, impl, ...)                                   \
+    do {                                                                  \
+        if (!(h)) {                                                       \
+            clear_error();                                                \
+            set_error("%s: null context", __func__);                      \
+            return CTBB_ERR_ARGUMENT;                                     \
+        }                                                                 \
+        return impl((h)->c, __VA_ARGS__);                                 \
+    } while (0)
+
+extern "C" int ctbb_context_reconstruct_scan_device(ctbb_context h, struct recon_metadata *mr, const float *d_scan,
+                                                    float *d_final, float mu_water)
+{
+    CTBB_CONTEXT_CALL(h, reconstruct_scan_device_in, mr, d_scan, d_final, mu_water);
+}
+
+extern "C" int ctbb_context_reconstruct_scan_host(ctbb_context h, struct recon_metadata *mr, const float *h_scan,
+                                                  float *h_final, float mu_water)
+{
+    CTBB_CONTEXT_CALL(h, reconstruct_scan_host_in, mr, h_scan, h_final, mu_water);
+}
+
+extern "C" int ctbb_context_reconstruct_scan_file(ctbb_context h, struct recon_metadata *mr, float *h_final,
+                                                  float mu_water)
+{
+    CTBB_CONTEXT_CALL(h, reconstruct_scan_file_in, mr, h_final, mu_water);
+}
+
+extern "C" int ctbb_context_reconstruct_device(ctbb_context h, struct recon_metadata *mr, const float *d_scan,
+                                               float *d_final, float mu_water)
+{
+    CTBB_CONTEXT_CALL(h, reconstruct_device_in, mr, d_scan, d_final, mu_water);
+}
+
+extern "C" int ctbb_context_reconstruct_host(ctbb_context h, struct recon_metadata *mr, const float *h_scan,
+                                             float *h_final, float mu_water)
+{
+    CTBB_CONTEXT_CALL(h, reconstruct_host_in, mr, h_scan, h_final, mu_water);
 }

@@ -46,6 +46,21 @@ PROTOTYPES = {
     "ctbb_rebin_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_ramp_filter_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),
+    "ctbb_scan_workspace_bytes": (C.c_size_t, [_MR]),
+    "ctbb_server_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "ctbb_server_submit": (C.c_int, [C.c_void_p, _MR, _F, _F, C.c_float, C.POINTER(C.c_uint64)]),
+    "ctbb_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, _VP]),
+    "ctbb_server_destroy": (C.c_int, [C.c_void_p]),
+    "ctbb_context_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "ctbb_context_destroy": (C.c_int, [C.c_void_p]),
+    "ctbb_context_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ctbb_context_release_workspace": (C.c_int, [C.c_void_p]),
+    "ctbb_context_device_bytes": (C.c_size_t, [C.c_void_p]),
+    "ctbb_context_reconstruct_scan_device": (C.c_int, [C.c_void_p, _MR, _VP, _VP, C.c_float]),
+    "ctbb_context_reconstruct_scan_host": (C.c_int, [C.c_void_p, _MR, _F, _F, C.c_float]),
+    "ctbb_context_reconstruct_scan_file": (C.c_int, [C.c_void_p, _MR, _F, C.c_float]),
+    "ctbb_context_reconstruct_device": (C.c_int, [C.c_void_p, _MR, _VP, _VP, C.c_float]),
+    "ctbb_context_reconstruct_host": (C.c_int, [C.c_void_p, _MR, _F, _F, C.c_float]),
     "ctbb_write_dicom_series": (C.c_int, [_MR, _F, C.c_int, C.c_float, C.c_char_p]),
     "ctbb_finalize_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
     "ctbb_reconstruct_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),

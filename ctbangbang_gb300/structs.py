@@ -164,3 +164,13 @@ def layout_offsets():
         ReconParams.nx.offset, ReconParams.table_dir.offset, ReconInfo.cb.offset,
         CtGeom.table_direction.offset,
     ]
+
+
+class RequestResult(C.Structure):
+    """struct ctbb_request_result (a finished server request)."""
+    _fields_ = [
+        ("status", C.c_int), ("worker", C.c_int), ("device_bytes", C.c_size_t),
+        ("queue_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
+        ("start_ms", C.c_double), ("end_ms", C.c_double),
+        ("error", C.c_char * 256),
+    ]

@@ -433,6 +433,84 @@ struct ctbb_phantom_object {
     float rotation[9];          /* row-major world->body rotation */
 };
 
+/* ---- contexts: concurrent scans ----------------------------------------
+   The reference keeps its state in per-translation-unit globals and runs one
+   scan at a time.  Every entry point above uses one library-wide context
+   (work buffers, tables, streams), serialised by a mutex.  A ctbb_context
+   holds its own work buffers, tables and streams, so scans on different
+   contexts run concurrently (from different host threads), their copies and
+   kernels overlapping on the GPU; calls on one context are serialised.  The
+   result of a scan does not depend on the context it ran on or on what runs
+   beside it.  A context is bound to the device current at its creation and
+   issues its work on a non-blocking stream of its own (or the caller's, after
+   ctbb_context_set_stream).  No counterpart in the reference. */
+typedef struct ctbb_context_s *ctbb_context;
+
+int ctbb_context_create(ctbb_context *out);
+/* Frees the context's device memory, streams and events; null is a no-op. */
+int ctbb_context_destroy(ctbb_context ctx);
+/* Issue the context's work on the caller's stream from now on. */
+int ctbb_context_set_stream(ctbb_context ctx, void *stream);
+/* Frees the context's work buffers (kept and reused between calls otherwise). */
+int ctbb_context_release_workspace(ctbb_context ctx);
+/* Device bytes the context's work buffers hold now. */
+size_t ctbb_context_device_bytes(ctbb_context ctx);
+/* ctbb_reconstruct_scan_device / _scan_host / _scan_file / ctbb_reconstruct_device /
+   ctbb_reconstruct_host on the context's buffers and stream. */
+int ctbb_context_reconstruct_scan_device(ctbb_context ctx, struct recon_metadata *mr,
+                                         const float *d_scan, float *d_final, float mu_water);
+int ctbb_context_reconstruct_scan_host(ctbb_context ctx, struct recon_metadata *mr,
+                                       const float *h_scan, float *h_final, float mu_water);
+int ctbb_context_reconstruct_scan_file(ctbb_context ctx, struct recon_metadata *mr,
+                                       float *h_final, float mu_water);
+int ctbb_context_reconstruct_device(ctbb_context ctx, struct recon_metadata *mr,
+                                    const float *d_scan, float *d_final, float mu_water);
+int ctbb_context_reconstruct_host(ctbb_context ctx, struct recon_metadata *mr,
+                                  const float *h_scan, float *h_final, float mu_water);
+
+/* Device bytes the whole-scan entry points hold for this plan (the union
+   window raw and filtered, its rebinned rows, the adaptive filter's
+   statistics, the image and final stacks, 8 MiB of tables and slack); 0 if
+   the plan is not usable.  Host only. */
+size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr);
+
+/* ---- request server: continuous batching of whole scans -----------------
+   n_workers threads, each with its own context, take requests first in first
+   out; a free worker starts the head request as soon as its device memory
+   (ctbb_scan_workspace_bytes) fits device_budget_bytes next to what the other
+   workers hold, so requests that arrive while others run are admitted as
+   slots and memory free up and overlap them on the GPU.  Workers keep their
+   buffers between requests; when a request does not fit, a worker drops its
+   own buffers and asks idle workers to drop theirs.  Each request runs
+   ctbb_context_reconstruct_scan_host: same result as ctbb_reconstruct_scan_host
+   alone.  No counterpart in the reference. */
+typedef struct ctbb_server_s *ctbb_server;
+
+struct ctbb_request_result {
+    int status;            /* ctbb_status of the reconstruction            */
+    int worker;            /* worker that ran it                           */
+    size_t device_bytes;   /* the request's device memory in the budget    */
+    double queue_ms;       /* submission -> start                          */
+    double run_ms;         /* start -> end                                 */
+    double latency_ms;     /* submission -> end                            */
+    double start_ms;       /* start, in ms since the server was created    */
+    double end_ms;         /* end, same clock                              */
+    char error[256];       /* ctbb_last_error() of a failed request        */
+};
+
+int ctbb_server_create(int n_workers, size_t device_budget_bytes, ctbb_server *out);
+/* Queue one scan: mr planned (configure_*; not shared with another request in
+   flight), h_scan [n_readings][n_rows_raw][n_channels] (pinned host memory
+   lets the copies overlap), h_final [n_slices_final][ny][nx].  A scan needing
+   more than the budget is refused (CTBB_ERR_ALLOC). */
+int ctbb_server_submit(ctbb_server srv, struct recon_metadata *mr, const float *h_scan,
+                       float *h_final, float mu_water, uint64_t *ticket);
+/* Block until the request is done; returns its status (and fills *out if
+   not null).  Each ticket is waited for once. */
+int ctbb_server_wait(ctbb_server srv, uint64_t ticket, struct ctbb_request_result *out);
+/* Finish the queued requests, stop the workers, free their contexts. */
+int ctbb_server_destroy(ctbb_server srv);
+
 /* Forward-project n_objects into frames [frame0, frame0+n_frames) of a helical
    FFS scan described by mr->cg / mr->rp and the tables mr->tube_angles,
    mr->table_positions (length rp.n_readings).  i0 > 0 adds Poisson noise with

@@ -62,6 +62,26 @@ def test_compute_entry_points_fail_loudly_without_gpu(lib, tmp_path):
         assert b"no CUDA device" in lib.ctbb_last_error()
     with pytest.raises(L.CtbbError):
         L.call("ctbb_rebin_filter", C.byref(mr))
+    h = C.c_void_p()
+    assert L.STATUS[lib.ctbb_context_create(C.byref(h))] == "CTBB_ERR_NO_DEVICE" and not h.value
+    assert L.STATUS[lib.ctbb_server_create(2, C.c_size_t(1 << 30), C.byref(h))] == "CTBB_ERR_NO_DEVICE"
+    assert not h.value
+    scans.free_plan(mr)
+
+
+def test_scan_workspace_bytes_counts_the_union_window(lib, tmp_path):
+    """The whole-scan footprint (the request server's admission unit): two
+    copies of the union window's raw frames, its rebinned rows, the image
+    and final stacks; more than one block's window, less than two scans."""
+    spec = scans.tiny(1, 1, n_slices=14, slice_thickness=2.5, seed=3)
+    mr = scans.plan_spec(spec, str(tmp_path))
+    need = lib.ctbb_scan_workspace_bytes(C.byref(mr))
+    assert mr.ri.n_blocks >= 2
+    frame = mr.cg.n_rows_raw * mr.cg.n_channels * 4
+    block_ws = lib.ctbb_workspace_bytes(C.byref(mr))
+    assert need > 2 * mr.ri.n_proj_pull * frame
+    assert need < 4 * spec.n_readings * frame + block_ws + (16 << 20)
+    assert lib.ctbb_scan_workspace_bytes(None) == 0
     scans.free_plan(mr)
 
 
