@@ -61,6 +61,13 @@ def parse_args():
     ap.add_argument("--path", choices=["scan", "blocks"], default="scan",
                     help="scan: one resident rebinned scan for all blocks (ctbb_reconstruct_scan_*); "
                          "blocks: the reference's block loop (ctbb_reconstruct_device / _host)")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the served-stream measurement (request server vs the plain per-scan path)")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-scans", type=int, default=8, help="distinct scans the requests draw from")
+    ap.add_argument("--serve-workers", type=int, default=3)
+    ap.add_argument("--serve-full", action="store_true",
+                    help="the full size distribution (up to 30 rotations, 300 slices) instead of the capped one")
     ap.add_argument("--profile-case", action="store_true",
                     help="one block of the config through each stage once (small case for ncu captures)")
     return ap.parse_args()
@@ -554,6 +561,14 @@ def run_ours(args):
             gbs = stage_bytes[name] / (t_launch * 1e-3) / 1e9
             entry.update({"achieved_gbs": gbs, "frac_of_hbm": gbs / hbm})
         stages[name] = entry
+    serve = None
+    if world == 1 and not args.no_serve:
+        del d_scan
+        torch.cuda.empty_cache()
+        try:
+            serve = serve_measure(args, torch)
+        except Exception as e:  # reported in the line, the rest of the run stands
+            serve = {"error": "%s: %s" % (type(e).__name__, e)}
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(spec, mr, blocks, sizes, steps=1, warmup=0)
@@ -589,6 +604,7 @@ def run_ours(args):
         "e2e": e2e,
         "other_path": whole,
         "e2e_file": e2e_file,
+        "serve": serve,
         "gpu_launches": launches / args.steps,
         "clocks": clk,
     }
@@ -596,6 +612,152 @@ def run_ours(args):
     scans.free_plan(mr)
     if dist is not None:
         dist.destroy_process_group()
+
+
+SERVE_CONFIG = 4  # the served stream: scan i is seeded 1000 * 4 + i
+
+
+def serve_spec(rng, i, full):
+    """One scan of the batched / served size distribution: FFS none / phi /
+    z / both, 16 / 32 / 64 rows (after z-FFS), pitch 0.6-1.5, rotations 2-30,
+    field 250-500 mm, 256^2 or 512^2, 20-300 slices of 1 mm, I0 2e4-2e5.
+    Without `full`, rotations are capped at 8 and slices at 120 (the default
+    bench run stays within minutes).  The slice count shrinks until the
+    rotations cover every block's pull window."""
+    from ctbangbang_gb300 import scans
+    z_ffs, phi_ffs = [(0, 0), (0, 1), (1, 0), (1, 1)][int(rng.integers(4))]
+    rows = int(rng.choice([16, 32, 64]))
+    pitch = float(rng.uniform(0.6, 1.5))
+    turns = int(rng.integers(2, 31 if full else 9))
+    fov = float(rng.uniform(250.0, 500.0))
+    nx = int(rng.choice([256, 512]))
+    n_slices = int(rng.integers(20, 301 if full else 121))
+    i0 = float(10.0 ** rng.uniform(math.log10(2e4), math.log10(2e5)))
+    spec = scans.ScanSpec(name="serve%d" % i, **scans._definition_as(), n_rows=rows, coll=0.6, pitch=pitch,
+                          turns=turns, slice_thickness=1.0, recon_fov=fov, nx=nx, ny=nx, start_pos=0.0,
+                          n_slices=n_slices, z_ffs=z_ffs, phi_ffs=phi_ffs, adaptive_filtration=1.0,
+                          seed=1000 * SERVE_CONFIG + i, n_ellipsoids=30, i0=i0)
+    spec.start_pos = scans.allowed_margin(spec) + 1.0
+    while spec.n_slices > 4 and scans.needed_turns(spec) > turns:
+        spec.n_slices = int(spec.n_slices * 0.85)
+    spec.turns = max(float(turns), scans.needed_turns(spec))
+    return spec
+
+
+def percentile(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
+
+
+def serve_measure(args, torch):
+    """The request server (ctbb_server_*) against the plain per-scan path on
+    the same requests: each request is one of `serve_scans` distinct scans
+    (own plan, own output).  Plain: every request alone through
+    ctbb_reconstruct_scan_host, one after another.  Served: all requests
+    submitted at once to a server of `serve_workers` workers (throughput),
+    then as a Poisson stream (latency); the plain path's latency under the
+    same arrivals is its FIFO queue over the measured per-scan times.  Every
+    served stack must equal its scan's stack alone."""
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+    from ctbangbang_gb300.serving import Server
+    lib = L.load()
+    rng = np.random.default_rng(1000 * SERVE_CONFIG)
+    tmp = tempfile.TemporaryDirectory(prefix="ctbb_serve_")
+    specs, prms, host, finals, vus = [], [], [], [], []
+    for i in range(args.serve_scans):
+        spec = serve_spec(rng, i, args.serve_full)
+        wd = os.path.join(tmp.name, str(i))
+        os.makedirs(wd)
+        prm, inst = scans.prepare(spec, wd)
+        mr = scans.plan(prm, inst)
+        n, frame = spec.n_readings, mr.cg.n_rows_raw * mr.cg.n_channels
+        ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
+        tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
+        objs = scans.phantom_objects(spec)
+        d = torch.empty(n * frame, dtype=torch.float32, device="cuda")
+        L.call("ctbb_phantom_project_device", C.byref(mr), objs, len(objs), C.c_void_p(ta.data_ptr()),
+               C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), spec.seed, C.c_void_p(d.data_ptr()))
+        h = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
+        h.copy_(d)
+        del d, ta, tp
+        n_final = lib.ctbb_n_slices_final(C.byref(mr))
+        specs.append(spec)
+        prms.append((prm, inst))
+        host.append(h)
+        finals.append(n_final * mr.rp.nx * mr.rp.ny)
+        vus.append(workload_sizes(mr, block_plans(mr))["vu_total"])
+        scans.free_plan(mr)
+    torch.cuda.empty_cache()
+    fptr = lambda t: t.numpy().ctypes.data_as(C.POINTER(C.c_float))
+    # plain: each scan alone (one warm-up, one timed run); its stack is the reference
+    alone, t_alone = [], []
+    for k in range(len(specs)):
+        mr = scans.plan(*prms[k])
+        out = torch.empty(finals[k], dtype=torch.float32, pin_memory=True)
+        L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(host[k]), fptr(out), C.c_float(0.0))
+        t0 = time.perf_counter()
+        L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(host[k]), fptr(out), C.c_float(0.0))
+        t_alone.append((time.perf_counter() - t0) * 1e3)
+        alone.append(out)
+        scans.free_plan(mr)
+    pick = [int(k) for k in rng.integers(len(specs), size=args.serve_requests)]
+    plain_ms = sum(t_alone[k] for k in pick)
+    free, total = torch.cuda.mem_get_info()
+    budget = int(min(150 << 30, 0.8 * free))
+
+    def run_stream(srv, arrivals):
+        mrs = [scans.plan(*prms[k]) for k in pick]
+        outs = [torch.empty(finals[k], dtype=torch.float32, pin_memory=True) for k in pick]
+        t0 = time.perf_counter()
+        tickets = []
+        for r, k in enumerate(pick):
+            if arrivals is not None:
+                delay = arrivals[r] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+            tickets.append(srv.submit(mrs[r], fptr(host[k]), fptr(outs[r])))
+        res = [srv.wait(t) for t in tickets]
+        wall = (time.perf_counter() - t0) * 1e3
+        same = all(torch.equal(outs[r], alone[k]) for r, k in enumerate(pick))
+        for m in mrs:
+            scans.free_plan(m)
+        return res, wall, same
+
+    with Server(args.serve_workers, budget) as srv:
+        run_stream(srv, None)  # workers size their buffers
+        res_sat, wall_sat, same_sat = run_stream(srv, None)
+        served_rate = len(pick) / (wall_sat * 1e-3)
+        rate = min(20.0, max(2.0, 0.8 * served_rate))
+        gaps = rng.exponential(1.0 / rate, size=len(pick))
+        arrivals = np.cumsum(gaps) - gaps[0]
+        res_poi, wall_poi, same_poi = run_stream(srv, arrivals)
+    lat = [r.latency_ms for r in res_poi]
+    # the plain path under the same arrivals: one scan at a time, first come first served
+    done, plain_lat = 0.0, []
+    for r, k in enumerate(pick):
+        start = max(arrivals[r] * 1e3, done)
+        done = start + t_alone[k]
+        plain_lat.append(done - arrivals[r] * 1e3)
+    vu = sum(vus[k] for k in pick)
+    desc = ["%s rows %d%s, %.1f rot, pitch %.2f, %d^2, %d slices, fov %.0f" % (
+        {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(s.z_ffs, s.phi_ffs)],
+        s.n_rows, "", s.turns, s.pitch, s.nx, s.n_slices, s.recon_fov) for s in specs]
+    return {
+        "workload": "%d requests drawn from %d seeded scans of the batched / served distribution%s" % (
+            len(pick), len(specs), "" if args.serve_full else " (rotations <= 8, slices <= 120)"),
+        "scans": desc,
+        "workers": args.serve_workers, "budget_gb": budget / 2**30,
+        "plain_scans_per_s": len(pick) / (plain_ms * 1e-3),
+        "served_scans_per_s": served_rate,
+        "served_vs_plain": served_rate / (len(pick) / (plain_ms * 1e-3)),
+        "served_voxel_updates_per_s": vu / (wall_sat * 1e-3),
+        "poisson_rate_per_s": rate,
+        "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99)},
+        "plain_latency_ms_same_arrivals": {"p50": percentile(plain_lat, 0.5), "p99": percentile(plain_lat, 0.99)},
+        "matches_alone": bool(same_sat and same_poi),
+        "entry_points": "ctbb_server_create / _submit / _wait (server) vs ctbb_reconstruct_scan_host (plain)",
+    }
 
 
 def run_profile_case(args):

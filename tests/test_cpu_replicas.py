@@ -3,6 +3,7 @@ torchrun): the slowest rank's time is what every rank reports, each replica
 reconstructs its own seeded scan, and the reference arm runs on rank 0 only.
 The ranks here are gloo processes on the host; no GPU is used."""
 import ast
+import ctypes as C
 import os
 import subprocess
 import sys
@@ -54,3 +55,28 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""
+
+
+def test_served_stream_scans_plan_and_fit(lib):
+    """The served-stream workload's scans (bench.serve_spec): every draw plans,
+    covers its slices and has a whole-scan footprint under the 150 GB budget."""
+    import tempfile
+
+    import numpy as np
+
+    import bench
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+    rng = np.random.default_rng(1000 * bench.SERVE_CONFIG)
+    modes = set()
+    for i in range(8):
+        spec = bench.serve_spec(rng, i, False)
+        assert spec.turns <= 8.5 and 4 <= spec.n_slices <= 120
+        modes.add((spec.z_ffs, spec.phi_ffs))
+        with tempfile.TemporaryDirectory() as d:
+            mr = scans.plan_spec(spec, d)
+            need = L.load().ctbb_scan_workspace_bytes(C.byref(mr))
+            assert 0 < need < (150 << 30)
+            assert mr.ri.n_blocks >= 1
+            scans.free_plan(mr)
+    assert len(modes) >= 3
