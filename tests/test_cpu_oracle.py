@@ -159,3 +159,22 @@ def test_interp_edge_rules_match_reference(oracle_lib, ref_lib):
                 x = oracle_lib.oracle_interp3(p, 6, 5, 4, i1, i2, i3)
                 y = ref_lib.ref_interp3(p, 6, 5, 4, i1, i2, i3)
                 assert x == y or (np.isnan(x) and np.isnan(y))
+
+
+@pytest.mark.parametrize("z_ffs,phi_ffs", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_fp32_reference_path_vs_fp64_oracle(lib, oracle_lib, tmp_path, z_ffs, phi_ffs):
+    """The reference's FP32 arithmetic (the oracle's float template) against
+    its FP64 template on one block: the precision the reference path itself
+    has, against which the GPU's 1 HU / 0.1 HU bars are set."""
+    spec = scans.tiny(z_ffs, phi_ffs, adaptive_filtration=3.0, seed=200 + 2 * z_ffs + phi_ffs)
+    scan = H.Scan(spec, str(tmp_path))
+    raw = scan.next_block()
+    f32 = H.oracle_block(oracle_lib, scan, raw)["block"].astype(np.float64)
+    taps = H.taps_of(scan.mr)
+    f64 = np.zeros(f32.size, np.float64)
+    oracle_lib.oracle64_block(C.byref(scan.mr), raw.ctypes.data_as(C.POINTER(C.c_float)), 1,
+                              taps.ctypes.data_as(C.POINTER(C.c_float)), f64.ctypes.data_as(C.POINTER(C.c_double)))
+    mx, rms = H.hu_errors(f32, f64)
+    assert np.abs(f64).max() > 0.01
+    assert mx <= 0.1 and rms <= 0.01, (mx, rms)
+    scan.close()

@@ -107,6 +107,34 @@ def test_backproject_hu(torch_cuda, oracle_lib, mode_scan):
     assert_hu(d_blk.cpu().numpy(), st["block"])
 
 
+def fp64_block(oracle_lib, mr, raw):
+    """The FP64 oracle's block (adaptive filter always, as main.cu:222 calls it)."""
+    taps = H.taps_of(mr)
+    out = np.zeros(H.dims(mr)["n_block"], np.float64)
+    oracle_lib.oracle64_block(C.byref(mr), fptr(np.ascontiguousarray(raw, np.float32)), 1, fptr(taps),
+                              out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def test_end_to_end_vs_fp64_oracle(torch_cuda, oracle_lib, mode_scan):
+    """The drop-in chain (adaptive filter, rebin + ramp filter,
+    backprojection) against the FP64 oracle of the same block: the bars of the
+    FP32 reference path apply (the reference's own FP32 path is within
+    0.02 HU of FP64 on these scans)."""
+    mr = mode_scan.mr
+    raw = mode_scan.next_block()
+    want = fp64_block(oracle_lib, mr, raw)
+    mode_scan.set_raw(raw)
+    L.call("ctbb_adaptive_filter_kk", C.byref(mr))
+    L.call("ctbb_rebin_filter", C.byref(mr))
+    L.call("ctbb_backproject", C.byref(mr))
+    d = H.dims(mr)
+    got = H.view(mr.ctd.image, d["n_image"])[:d["n_block"]].astype(np.float64)
+    assert np.abs(want).max() > 0.01
+    mx, rms = assert_hu(got, want)
+    print("GPU vs FP64 oracle: max %.4f HU, rms %.5f HU" % (mx, rms))
+
+
 def run_dropin(scan):
     """main.cu's block loop and finalize through the drop-in entry points."""
     mr = scan.mr
