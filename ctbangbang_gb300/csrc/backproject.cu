@@ -22,9 +22,9 @@
 // GB300 mapping: one thread per (x, y) column and ZPT (8) consecutive
 // slices, 128-thread CTAs of 32 x 4 columns, each warp an 8 x 4 tile so that
 // its gathers fall on few detector channels.  Per angle i the asin and root
-// of the k = 0 view serve all half turns (p only changes sign), and a
-// warp-uniform window limits k to the half turns whose rays can reach the
-// chunk.  Per visited (i, k) the geometry is computed once for the chunk,
+// of the k = 0 view are carried to every half turn to first order in |p|
+// (the reference's half turns are pi', not pi, apart), and a warp-uniform
+// window limits k to the half turns whose rays can reach the chunk.  Per visited (i, k) the geometry is computed once for the chunk,
 // which a warp vote classes as flat (W = 1), inner (all |q| < 1) or other
 // (window edge, clamps, last-turn border); slices run in pairs with packed
 // FP32 (FFMA2 / FADD2 / FMUL2); the per-angle sums s, h stay in registers and
@@ -209,18 +209,30 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             s2[m] = make_float2(0.0f, 0.0f);
             h2[m] = make_float2(0.0f, 0.0f);
         }
-        // The views i + k n_half are half turns apart: p flips its sign from
-        // one to the next and |p| stays, so asin(|p| / r_f) and sqrt(r_f^2 - p^2)
-        // are taken once per angle (from k = 0) and given the sign of each p.
+        // The views i + k n_half are nearly half turns apart: p nearly flips
+        // its sign from one to the next.  Not exactly: the reference steps
+        // half turns by pi' = 3.1415368979, so view k is turned a further
+        // k (pi - pi') = k 5.6e-5 rad and |p_k| differs from |p_0| by up to
+        // k r 5.6e-5 (0.04 mm at the corner of a 500 mm field, 1e-3 detector
+        // rows in q at config-3 geometry).  asin(|p| / r_f) and
+        // sqrt(r_f^2 - p^2) are taken once per angle at |p_0| and carried to
+        // each |p_k| to first order: d = |p_k| - |p_0|, asin += d / root,
+        // root -= (|p_0| / root) d (second-order terms below 1e-8 rad), with
+        // the constants folded: asin_k = |p_k| / root + A, root_k = B - s |p_k|.
         const float4 *vt = p.views + (size_t)i * p.nht;
-        float a_abs, root;
+        float a_abs, root, inv_root, slope, a_off, root_off;
         int k_lo = 0, k_hi = p.nht - 1;
         {
             float4 t0 = __ldg(vt);
             float phat0 = __fsub_rn(__fmul_rn(x, t0.y), __fmul_rn(y, t0.z));
             a_abs = fabsf(asin_fast(phat0 * p.inv_rf));
             float l2 = fmaf(-phat0, phat0, p.rf2);
-            root = l2 * rsqrtf(l2);
+            inv_root = rsqrtf(l2);
+            root = l2 * inv_root;
+            const float p0_abs = fabsf(phat0);
+            slope = p0_abs * inv_root;
+            a_off = fmaf(-p0_abs, inv_root, a_abs);
+            root_off = fmaf(slope, p0_abs, root);
             if (p.k_window) {
                 // Half turns whose rays can reach the chunk: ray_k lies within
                 // |asin zr| of (theta_0 + k pi') zr, and |q| < 1 needs
@@ -242,9 +254,12 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             float4 t = __ldg(vt + k);
             // q of the chunk's slices: q(z) = q0 + z dq (dq > 0)
             float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
+            // this view's asin(|p| / r_f) and sqrt(r_f^2 - p^2) from the angle's
+            const float a_k = fmaf(fabsf(phat), inv_root, a_off);
+            const float root_k = fmaf(-slope, fabsf(phat), root_off);
             // zbase - ray with ray = (theta - asin(p / r_f)) z_rot / 2 pi'
-            float zb_ray = fmaf(copysignf(a_abs, phat), p.zrot_over_2pi, zbase - t.w);
-            float lhat = root - x * t.z - y * t.y;
+            float zb_ray = fmaf(copysignf(a_k, phat), p.zrot_over_2pi, zbase - t.w);
+            float lhat = root_k - x * t.z - y * t.y;
             float inv_den = __fdividef(1.0f, lhat * p.tan_cone);
             float q0 = zb_ray * inv_den;
             float dq = p.coll * inv_den;

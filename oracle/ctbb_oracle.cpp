@@ -663,6 +663,19 @@ int oracle64_block(const struct recon_metadata *mr, const float *raw, int adapti
     return 0;
 }
 
+/* Backprojection of angles [i0, i1) of the block from float filtered rows
+   [n_views][n_rows][n_os], in double, into out_block (overwritten). */
+int oracle64_backproject_range(const struct recon_metadata *mr, const float *rows, int i0, int i1,
+                               double *out_block)
+{
+    size_t nv = n_views_of(*mr);
+    std::vector<double> rb(rows, rows + nv * mr->cg.n_rows * mr->cg.n_channels_oversampled);
+    size_t block = (size_t)mr->rp.nx * mr->rp.ny * mr->ri.n_slices_block;
+    std::fill(out_block, out_block + block, 0.0);
+    backproject<double>(*mr, rb.data(), i0, i1, out_block);
+    return 0;
+}
+
 int oracle64_finalize(const struct recon_metadata *mr, const double *image, double *final_out)
 {
     finalize<double>(*mr, image, final_out);

@@ -312,17 +312,21 @@ def test_config1_geometry_reduced_image(torch_cuda, oracle_lib, lib, tmp_path):
     scan.close()
 
 
-def test_config2_geometry_backprojection(torch_cuda, oracle_lib, lib, tmp_path):
+@pytest.mark.parametrize("config", ["config2", "config3"])
+def test_config_geometry_backprojection(torch_cuda, oracle_lib, lib, tmp_path, config):
     """Backprojection of block 0 with the config-2 scanner and helix (1472 x 64
-    rebinned rows, 1152 views/turn, phi+z FFS, pitch 0.8) over the full 500 mm
-    field at 64^2 pixels: the rows the whole-scan benchmark reads, including
-    the flat (|q| <= Q) chunks that only detectors of 8 or more rows take.  The
+    rebinned rows, 1152 views/turn, phi+z FFS, pitch 0.8, 4 half turns per
+    window) or config 3's (1472 x 128 rows, 3 half turns) over the full 500 mm
+    field at 64^2 pixels: the rows the benchmarks read, including the flat
+    (|q| <= Q) chunks that only detectors of 8 or more rows take.  The
     filtered rows come from the device stages (checked against the oracle on
     the small scans above); the oracle backprojects the same rows."""
     torch = torch_cuda
     from ctbangbang_gb300 import structs
-    spec = scans.ScanSpec(**{**scans.CONFIGS["config2"].__dict__})
+    spec = scans.ScanSpec(**{**scans.CONFIGS[config].__dict__})
     spec.nx = spec.ny = 64
+    if config == "config3":
+        spec.turns, spec.n_slices = 6.0, 32  # block 0 only
     mr = scans.plan_spec(spec, str(tmp_path))
     L.call("ctbb_update_block_info", C.byref(mr))
     m = structs.ReconMetadata()
