@@ -312,21 +312,34 @@ def test_config1_geometry_reduced_image(torch_cuda, oracle_lib, lib, tmp_path):
     scan.close()
 
 
-@pytest.mark.parametrize("config", ["config2", "config3"])
-def test_config_geometry_backprojection(torch_cuda, oracle_lib, lib, tmp_path, config):
+GEOMETRY_CASES = {
+    "config2": ("config2", {}),
+    "config3": ("config3", {"turns": 6.0, "n_slices": 32}),  # block 0 only
+    # 6 half turns per window: the pi' drift of p grows with the half turn
+    "config2_pitch0.5": ("config2", {"pitch": 0.5, "turns": 14.0}),
+    "config2_in_offset": ("config2", {"table_dir": "in", "x_origin": 40.0, "y_origin": -25.0,
+                                      "tube_start_angle": 45.0}),
+}
+
+
+@pytest.mark.parametrize("case", list(GEOMETRY_CASES))
+def test_config_geometry_backprojection(torch_cuda, oracle_lib, lib, tmp_path, case):
     """Backprojection of block 0 with the config-2 scanner and helix (1472 x 64
     rebinned rows, 1152 views/turn, phi+z FFS, pitch 0.8, 4 half turns per
-    window) or config 3's (1472 x 128 rows, 3 half turns) over the full 500 mm
-    field at 64^2 pixels: the rows the benchmarks read, including the flat
-    (|q| <= Q) chunks that only detectors of 8 or more rows take.  The
-    filtered rows come from the device stages (checked against the oracle on
-    the small scans above); the oracle backprojects the same rows."""
+    window), config 3's (1472 x 128 rows, 3 half turns), config 2 at pitch 0.5
+    (6 half turns) or with the table moving in, an off-centre field and a 45
+    degree tube start, over the full 500 mm field at 64^2 pixels: the rows
+    the benchmarks read, including the flat (|q| <= Q) chunks that only
+    detectors of 8 or more rows take.  The filtered rows come from the device
+    stages (checked against the oracle on the small scans above); the oracle
+    backprojects the same rows."""
     torch = torch_cuda
     from ctbangbang_gb300 import structs
+    config, changes = GEOMETRY_CASES[case]
     spec = scans.ScanSpec(**{**scans.CONFIGS[config].__dict__})
     spec.nx = spec.ny = 64
-    if config == "config3":
-        spec.turns, spec.n_slices = 6.0, 32  # block 0 only
+    for k, v in changes.items():
+        setattr(spec, k, v)
     mr = scans.plan_spec(spec, str(tmp_path))
     L.call("ctbb_update_block_info", C.byref(mr))
     m = structs.ReconMetadata()
