@@ -49,6 +49,7 @@ struct Job {
     int status = CTBB_OK;
     int worker = -1;
     bool done = false;
+    bool waited = false;  // a ctbb_server_wait call owns it
     std::string error;
 };
 
@@ -74,6 +75,7 @@ struct ctbb_server_s {
     int device = 0;
     Clock::time_point created = Clock::now();
     bool stopping = false;
+    int waiters = 0;  // ctbb_server_wait calls in progress
     std::vector<Worker> workers;
 };
 
@@ -240,8 +242,16 @@ extern "C" int ctbb_server_wait(ctbb_server s, uint64_t ticket, struct ctbb_requ
         return CTBB_ERR_ARGUMENT;
     }
     Job *j = it->second;
+    if (j->waited) {
+        set_error("ctbb_server_wait: ticket %llu is already being waited for", (unsigned long long)ticket);
+        return CTBB_ERR_STATE;
+    }
+    j->waited = true;
+    ++s->waiters;
     s->done_cv.wait(lk, [j] { return j->done; });
-    s->jobs.erase(it);
+    s->jobs.erase(ticket);
+    --s->waiters;
+    s->done_cv.notify_all();  // a destroy may be waiting for the last waiter
     int st = j->status;
     if (out) {
         memset(out, 0, sizeof(*out));
@@ -271,6 +281,11 @@ extern "C" int ctbb_server_destroy(ctbb_server s)
     }
     for (Worker &w : s->workers)
         if (w.thread.joinable()) w.thread.join();
+    {
+        // every queued request has finished; let the waiters take their results
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->done_cv.wait(lk, [s] { return s->waiters == 0; });
+    }
     for (Worker &w : s->workers) ctbb_context_destroy(w.ctx);
     for (auto &kv : s->jobs) delete kv.second;
     delete s;

@@ -508,7 +508,9 @@ int ctbb_server_submit(ctbb_server srv, struct recon_metadata *mr, const float *
 /* Block until the request is done; returns its status (and fills *out if
    not null).  Each ticket is waited for once. */
 int ctbb_server_wait(ctbb_server srv, uint64_t ticket, struct ctbb_request_result *out);
-/* Finish the queued requests, stop the workers, free their contexts. */
+/* Finish the queued requests, let threads blocked in ctbb_server_wait take
+   their results, stop the workers, free their contexts.  No call on srv may
+   start after this one. */
 int ctbb_server_destroy(ctbb_server srv);
 
 /* Forward-project n_objects into frames [frame0, frame0+n_frames) of a helical

@@ -132,6 +132,16 @@ def test_server_budget_bounds_what_runs_together(torch_cuda, requests):
                 assert len(running) == 1, running
 
 
+def test_server_ticket_is_collected_once(torch_cuda, requests):
+    r = requests[1]
+    with Server(n_workers=2, device_budget_bytes=8 << 30) as srv:
+        t = srv.submit(r.scan.mr, fptr(r.h_scan), fptr(r.h_final))
+        assert srv.wait(t).status == 0
+        with pytest.raises(L.CtbbError) as e:
+            srv.wait(t)
+    assert e.value.status_name == "CTBB_ERR_ARGUMENT"
+
+
 def test_server_refuses_a_scan_over_the_budget(torch_cuda, requests):
     r = requests[0]
     need = L.load().ctbb_scan_workspace_bytes(C.byref(r.scan.mr))
