@@ -230,8 +230,9 @@ R get_beta_idx(R beta, const R *lookup, int n)
 }
 
 // rebin of the kept views: out[view][row][Nos] (no filter)
+// Views [v0, v1) of the block (v1 < 0: all); each view is independent.
 template <class R>
-void rebin(const struct recon_metadata &mr, const R *raw, R *out)
+void rebin(const struct recon_metadata &mr, const R *raw, R *out, int v0 = 0, int v1 = -1)
 {
     const struct ct_geom &cg = mr.cg;
     const struct recon_params &rp = mr.rp;
@@ -258,7 +259,7 @@ void rebin(const struct recon_metadata &mr, const R *raw, R *out)
         for (int c = 0; c < Nos; c++) {
             const R beta = std::asin(((R)c - 2 * cc) * (fai / 2));
             R beta_idx = beta / fai + cc;
-            for (int v = 0; v < V; v++) {
+            for (int v = v0; v < (v1 < 0 ? V : std::min(v1, V)); v++) {
                 int proj = v + add;
                 R alpha_idx = (R)proj - beta * (R)cg.n_proj_turn / (R(2) * pi);
                 for (int row = 0; row < Rout; row++)
@@ -280,7 +281,7 @@ void rebin(const struct recon_metadata &mr, const R *raw, R *out)
             lk1[i] = beta_rk<R>((R)da, (R)-dr, (R)i, 0, cg);
             lk2[i] = beta_rk<R>((R)da, (R)dr, (R)i, 0, cg);
         }
-        for (int v = 0; v < V; v++) {
+        for (int v = v0; v < (v1 < 0 ? V : std::min(v1, V)); v++) {
             int proj = v + add;
             for (int row = 0; row < Rr; row++)
                 for (int c = 0; c < Nos; c++) {
@@ -313,7 +314,7 @@ void rebin(const struct recon_metadata &mr, const R *raw, R *out)
             lookup[2 * ch] = beta_rk<R>((R)da, 0, (R)ch, 0, cg);
             lookup[2 * ch + 1] = beta_rk<R>((R)-da, 0, (R)ch, 0, cg);
         }
-        for (int v = 0; v < V; v++) {
+        for (int v = v0; v < (v1 < 0 ? V : std::min(v1, V)); v++) {
             int proj = v + add;
             for (int row = 0; row < Rr; row++)
                 for (int ch = 0; ch < N; ch++) {
@@ -354,7 +355,7 @@ void rebin(const struct recon_metadata &mr, const R *raw, R *out)
         lk2[2 * ch + 1] = beta_rk<R>(sda[3], sdr[3], (R)ch, 0, cg);
     }
     const R *lkq[4] = {&lk1[0], &lk1[1], &lk2[0], &lk2[1]};
-    for (int v = 0; v < V; v++) {
+    for (int v = v0; v < (v1 < 0 ? V : std::min(v1, V)); v++) {
         int proj = v + add;
         for (int row = 0; row < Rr; row++)
             for (int ch = 0; ch < N; ch++)
@@ -673,6 +674,14 @@ int oracle64_backproject_range(const struct recon_metadata *mr, const float *row
     size_t block = (size_t)mr->rp.nx * mr->rp.ny * mr->ri.n_slices_block;
     std::fill(out_block, out_block + block, 0.0);
     backproject<double>(*mr, rb.data(), i0, i1, out_block);
+    return 0;
+}
+
+/* Rebin (no filter) of views [v0, v1) of the block from a float raw window
+   [P][R_raw][N] into out [n_views][n_rows][n_os] (only those views written). */
+int oracle_rebin_views(const struct recon_metadata *mr, const float *raw, int v0, int v1, float *out)
+{
+    rebin<float>(*mr, raw, out, v0, v1);
     return 0;
 }
 

@@ -312,6 +312,53 @@ def test_config1_geometry_reduced_image(torch_cuda, oracle_lib, lib, tmp_path):
     scan.close()
 
 
+def test_config2_block_adaptive_filter_and_rebin_bit_exact(torch_cuda, oracle_lib, lib, tmp_path):
+    """Block 0 of the config-2 scan at full size (11264 frames of 32 x 736,
+    phi+z FFS, adaptive filter on: 18 and 180 degree statistics windows of
+    ~230 and ~2300 frames): the device adaptive filter against the oracle on
+    every sample, and the device rebin against the oracle on views at the
+    start, middle and end of the block -- bit for bit."""
+    torch = torch_cuda
+    from ctbangbang_gb300 import structs
+    spec = scans.ScanSpec(**{**scans.CONFIGS["config2"].__dict__})
+    spec.nx = spec.ny = 64
+    mr = scans.plan_spec(spec, str(tmp_path))
+    L.call("ctbb_update_block_info", C.byref(mr))
+    m = structs.ReconMetadata()
+    C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+    n = spec.n_readings
+    frame = m.cg.n_rows_raw * m.cg.n_channels
+    P = m.ri.n_proj_pull
+    d = H.dims(mr)
+    ta = dev(torch, np.ctypeslib.as_array(mr.tube_angles, (n,)).copy())
+    tp = dev(torch, np.ctypeslib.as_array(mr.table_positions, (n,)).copy())
+    objs = scans.phantom_objects(spec)
+    d_raw = torch.empty(P * frame, dtype=torch.float32, device="cuda")
+    L.call("ctbb_phantom_project_device", C.byref(m), objs, len(objs), ptr(ta), ptr(tp),
+           int(m.ri.idx_pull_start), P, C.c_float(spec.i0), spec.seed, ptr(d_raw))
+    d_filt = torch.empty_like(d_raw)
+    L.call("ctbb_adaptive_filter_device", C.byref(m), ptr(d_raw), ptr(d_filt))
+    d_rb = torch.empty(d["n_rebin"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_rebin_device", C.byref(m), ptr(d_filt), ptr(d_rb))
+    torch.cuda.synchronize()
+    raw = d_raw.cpu().numpy()
+    got_filt = d_filt.cpu().numpy()
+    del d_raw, d_filt
+    H.view(mr.ctd.raw, d["n_raw"])[:] = raw
+    oracle_lib.oracle_adaptive_filter(C.byref(mr))
+    want_filt = H.view(mr.ctd.raw, d["n_raw"]).copy()
+    assert (want_filt != raw).sum() > 1000  # the filter changed samples
+    np.testing.assert_array_equal(got_filt, want_filt)
+    nv = d["n_views"]
+    view = mr.cg.n_rows * mr.cg.n_channels_oversampled
+    want = np.zeros(d["n_rebin"], np.float32)
+    got = d_rb.cpu().numpy()
+    for v0 in (0, nv // 2 - 4, nv - 8):
+        oracle_lib.oracle_rebin_views(C.byref(mr), fptr(want_filt), v0, v0 + 8, fptr(want))
+        np.testing.assert_array_equal(got[v0 * view:(v0 + 8) * view], want[v0 * view:(v0 + 8) * view])
+    scans.free_plan(mr)
+
+
 GEOMETRY_CASES = {
     "config2": ("config2", {}),
     "config3": ("config3", {"turns": 6.0, "n_slices": 32}),  # block 0 only
