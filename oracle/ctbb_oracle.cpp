@@ -440,9 +440,12 @@ R tube_start_of(const struct recon_metadata &mr)
     return (R)(std::fmod(a, 360.0) * Pi<double>::bp / 180.0);
 }
 
-// Angles [i0, i1) of one block into out_block [n_slices_block][ny][nx] (added).
+// Angles [i0, i1) of one block into out_block [n_slices_block][ny][nx]
+// (added), for the pixels x in [x_lo, x_hi), y in [y_lo, y_hi) (x_hi, y_hi < 0:
+// to the edge); every pixel is independent of the others.
 template <class R>
-void backproject(const struct recon_metadata &mr, const R *rebin, int i0, int i1, R *out_block)
+void backproject(const struct recon_metadata &mr, const R *rebin, int i0, int i1, R *out_block, int x_lo = 0,
+                 int x_hi = -1, int y_lo = 0, int y_hi = -1)
 {
     const struct ct_geom &cg = mr.cg;
     const struct recon_params &rp = mr.rp;
@@ -460,9 +463,9 @@ void backproject(const struct recon_metadata &mr, const R *rebin, int i0, int i1
             std::memcpy(&proj[view * kk], &rebin[((size_t)i + (size_t)kk * cg.n_proj_turn / 2) * view], view * sizeof(R));
         std::fill(s_t.begin(), s_t.end(), R(0));
         std::fill(h_t.begin(), h_t.end(), R(0));
-        for (int xi = 0; xi < nx; xi++) {
+        for (int xi = x_lo; xi < (x_hi < 0 ? nx : x_hi); xi++) {
             R x = (fov / (R)rp.nx) * ((R)xi - (R)(rp.nx - 1) / R(2)) + (R)rp.x_origin;
-            for (int yi = 0; yi < ny; yi++) {
+            for (int yi = y_lo; yi < (y_hi < 0 ? ny : y_hi); yi++) {
                 R y = (fov / (R)rp.ny) * ((R)yi - (R)(rp.ny - 1) / R(2)) + (R)rp.y_origin;
                 for (int k = 0; k < nht; k++) {
                     R theta = tube_start + (R(2) * pi / (R)cg.n_proj_turn) * (R)i + (R)k * pi;
@@ -482,8 +485,8 @@ void backproject(const struct recon_metadata &mr, const R *rebin, int i0, int i1
                 }
             }
         }
-        for (int xi = 0; xi < nx; xi++)
-            for (int yi = 0; yi < ny; yi++)
+        for (int xi = x_lo; xi < (x_hi < 0 ? nx : x_hi); xi++)
+            for (int yi = y_lo; yi < (y_hi < 0 ? ny : y_hi); yi++)
                 for (int zi = 0; zi < nz; zi++) {
                     size_t o = (size_t)zi * nx * ny + (size_t)yi * nx + xi;
                     size_t in = (size_t)nz * ny * xi + (size_t)nz * yi + zi;
@@ -682,6 +685,19 @@ int oracle64_backproject_range(const struct recon_metadata *mr, const float *row
 int oracle_rebin_views(const struct recon_metadata *mr, const float *raw, int v0, int v1, float *out)
 {
     rebin<float>(*mr, raw, out, v0, v1);
+    return 0;
+}
+
+/* oracle_backproject_range for the pixels x in [x0, x1), y in [y0, y1) only
+   (out_block written there, zeroed first there). */
+int oracle_backproject_patch(const struct recon_metadata *mr, const float *rebin_data, int x0, int x1, int y0,
+                             int y1, float *out_block)
+{
+    const size_t nx = mr->rp.nx, ny = mr->rp.ny;
+    for (size_t z = 0; z < mr->ri.n_slices_block; ++z)
+        for (int y = y0; y < y1; ++y)
+            for (int x = x0; x < x1; ++x) out_block[(z * ny + (size_t)y) * nx + (size_t)x] = 0.0f;
+    backproject<float>(*mr, rebin_data, 0, (int)(mr->cg.n_proj_turn / 2), out_block, x0, x1, y0, y1);
     return 0;
 }
 

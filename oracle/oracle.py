@@ -65,6 +65,7 @@ def oracle():
             "oracle64_finalize": (C.c_int, [_MR, _D, _D]),
             "oracle64_backproject_range": (C.c_int, [_MR, _F, C.c_int, C.c_int, _D]),
             "oracle_rebin_views": (C.c_int, [_MR, _F, C.c_int, C.c_int, _F]),
+            "oracle_backproject_patch": (C.c_int, [_MR, _F, C.c_int, C.c_int, C.c_int, C.c_int, _F]),
             "oracle_interp2": (C.c_float, [_F, C.c_int, C.c_int, C.c_float, C.c_float]),
             "oracle_interp3": (C.c_float, [_F, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]),
         }

@@ -359,6 +359,50 @@ def test_config2_block_adaptive_filter_and_rebin_bit_exact(torch_cuda, oracle_li
     scans.free_plan(mr)
 
 
+def test_config2_block_backprojection_512_patches(torch_cuda, oracle_lib, lib, tmp_path):
+    """The benchmark's own image, config 2's block 0 at 512^2 over the full
+    field (a warp then covers 8 x 4 mm, so the flat / inner / other classes
+    mix as in the benchmark): the GPU block against the oracle on a 32 x 32
+    patch at the centre and one at the edge of the field, all 32 slices."""
+    torch = torch_cuda
+    from ctbangbang_gb300 import structs
+    spec = scans.ScanSpec(**{**scans.CONFIGS["config2"].__dict__})
+    mr = scans.plan_spec(spec, str(tmp_path))
+    L.call("ctbb_update_block_info", C.byref(mr))
+    m = structs.ReconMetadata()
+    C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+    n = spec.n_readings
+    frame = m.cg.n_rows_raw * m.cg.n_channels
+    P = m.ri.n_proj_pull
+    d = H.dims(mr)
+    ta = dev(torch, np.ctypeslib.as_array(mr.tube_angles, (n,)).copy())
+    tp = dev(torch, np.ctypeslib.as_array(mr.table_positions, (n,)).copy())
+    objs = scans.phantom_objects(spec)
+    d_raw = torch.empty(P * frame, dtype=torch.float32, device="cuda")
+    L.call("ctbb_phantom_project_device", C.byref(m), objs, len(objs), ptr(ta), ptr(tp),
+           int(m.ri.idx_pull_start), P, C.c_float(spec.i0), spec.seed, ptr(d_raw))
+    d_filt = torch.empty_like(d_raw)
+    L.call("ctbb_adaptive_filter_device", C.byref(m), ptr(d_raw), ptr(d_filt))
+    del d_raw
+    d_rb = torch.empty(d["n_rebin"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_rebin_device", C.byref(m), ptr(d_filt), ptr(d_rb))
+    del d_filt
+    taps = H.taps_of(m)
+    L.call("ctbb_ramp_filter_device", ptr(d_rb), d["n_views"] * m.cg.n_rows, m.cg.n_channels_oversampled, fptr(taps))
+    d_blk = torch.empty(d["n_block"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_backproject_device", C.byref(m), ptr(d_rb), ptr(d_blk))
+    torch.cuda.synchronize()
+    rows = d_rb.cpu().numpy()
+    got = d_blk.cpu().numpy().reshape(m.ri.n_slices_block, m.rp.ny, m.rp.nx)
+    want = np.zeros(d["n_block"], np.float32)
+    for x0, y0 in ((240, 240), (0, 240)):
+        oracle_lib.oracle_backproject_patch(C.byref(m), fptr(rows), x0, x0 + 32, y0, y0 + 32, fptr(want))
+        w = want.reshape(got.shape)[:, y0:y0 + 32, x0:x0 + 32]
+        assert np.abs(w).max() > 0.005
+        assert_hu(got[:, y0:y0 + 32, x0:x0 + 32], w)
+    scans.free_plan(mr)
+
+
 GEOMETRY_CASES = {
     "config2": ("config2", {}),
     "config3": ("config3", {"turns": 6.0, "n_slices": 32}),  # block 0 only
