@@ -220,6 +220,30 @@ def test_image_shapes_and_helices_vs_oracle(torch_cuda, oracle_lib, lib, tmp_pat
     scan.close()
 
 
+def test_zero_scan_reconstructs_to_zero(torch_cuda, oracle_lib, lib, tmp_path):
+    """An empty scan (no attenuation: every line integral 0, so the adaptive
+    filter's per-frame maxima are 0 and its eccentricity 0/0): every stage
+    stays finite and the stack is exactly 0, as in the reference arithmetic,
+    through the drop-in chain and the whole-scan path."""
+    torch = torch_cuda
+    spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=53)
+    scan = H.Scan(spec, str(tmp_path))
+    scan.frames[:] = 0
+    raw = scan.next_block()
+    st = H.oracle_block(oracle_lib, scan, raw)
+    assert not st["block"].any()
+    reset_blocks(scan)
+    img, fin = run_dropin(scan)
+    assert np.isfinite(img).all() and not img.any()
+    assert np.isfinite(fin).all() and not fin.any()
+    d_scan = dev(torch, scan.frames.reshape(-1))
+    d_fin = torch.full((fin.size,), float("nan"), dtype=torch.float32, device="cuda")
+    L.call("ctbb_reconstruct_scan_device", C.byref(scan.mr), ptr(d_scan), ptr(d_fin), 0.0)
+    out = d_fin.cpu().numpy()
+    assert np.isfinite(out).all() and not out.any()
+    scan.close()
+
+
 def test_reconstruct_device_equals_dropin(torch_cuda, lib, tmp_path):
     torch = torch_cuda
     spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=41)
