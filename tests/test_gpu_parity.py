@@ -199,12 +199,14 @@ def shape_spec(variant):
         return scans.tiny(1, 1, adaptive_filtration=2.0, pitch=0.6, n_slices=14, slice_thickness=2.5, seed=62)
     if variant == "pitch_1.4":
         return scans.tiny(1, 0, adaptive_filtration=2.0, pitch=1.4, seed=63)
+    if variant == "wide_detector":  # 4096 oversampled channels: 8192-point filter, runtime row stride
+        return scans.tiny(0, 1, adaptive_filtration=2.0, n_channels=2048, seed=71)
     spec = scans.tiny(1, 1, adaptive_filtration=2.0, nx=40, ny=40, seed=64)
     spec.x_origin, spec.y_origin, spec.tube_start_angle = 7.5, -4.0, 30.0
     return spec
 
 
-@pytest.mark.parametrize("variant", ["odd_image", "pitch_0.6", "pitch_1.4", "offset_origin"])
+@pytest.mark.parametrize("variant", ["odd_image", "pitch_0.6", "pitch_1.4", "offset_origin", "wide_detector"])
 def test_image_shapes_and_helices_vs_oracle(torch_cuda, oracle_lib, lib, tmp_path, variant):
     """Image sides off the thread tiling, other pitches, an off-centre field
     of view with a rotated tube start: the drop-in block loop against the
@@ -241,6 +243,34 @@ def test_zero_scan_reconstructs_to_zero(torch_cuda, oracle_lib, lib, tmp_path):
     L.call("ctbb_reconstruct_scan_device", C.byref(scan.mr), ptr(d_scan), ptr(d_fin), 0.0)
     out = d_fin.cpu().numpy()
     assert np.isfinite(out).all() and not out.any()
+    scan.close()
+
+
+def test_large_image_backprojection_patches(torch_cuda, oracle_lib, lib, tmp_path):
+    """A 1024^2 image (a 512 x 256 CTA grid): the GPU backprojection of the
+    oracle's filtered rows against the oracle's on a corner and a centre patch."""
+    torch = torch_cuda
+    scan = H.Scan(scans.tiny(1, 1, adaptive_filtration=2.0, nx=1024, ny=1024, seed=72), str(tmp_path))
+    mr = scan.mr
+    scan.next_block()
+    d = H.dims(mr)
+    # the oracle's filtered rows (its backprojection of the whole image would
+    # take minutes; only the patches below are backprojected)
+    oracle_lib.oracle_adaptive_filter(C.byref(mr))
+    oracle_lib.oracle_rebin(C.byref(mr))
+    rows = H.view(mr.ctd.rebin, d["n_rebin"]).copy()
+    oracle_lib.oracle_filter_rows(fptr(rows), d["n_views"] * mr.cg.n_rows, mr.cg.n_channels_oversampled,
+                                  fptr(H.taps_of(mr)))
+    d_blk = torch.empty(d["n_block"], dtype=torch.float32, device="cuda")
+    L.call("ctbb_backproject_device", C.byref(mr), ptr(dev(torch, rows)), ptr(d_blk))
+    torch.cuda.synchronize()
+    got = d_blk.cpu().numpy().reshape(mr.ri.n_slices_block, 1024, 1024)
+    want = np.zeros(d["n_block"], np.float32)
+    for x0, y0 in ((0, 0), (496, 504), (992, 960)):
+        oracle_lib.oracle_backproject_patch(C.byref(mr), fptr(rows), x0, x0 + 32, y0, y0 + 32, fptr(want))
+        w = want.reshape(got.shape)[:, y0:y0 + 32, x0:x0 + 32]
+        assert_hu(got[:, y0:y0 + 32, x0:x0 + 32], w)
+    assert np.abs(want).max() > 0.005
     scan.close()
 
 
