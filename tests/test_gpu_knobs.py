@@ -1,0 +1,80 @@
+"""GPU tests of the environment knobs (read once per process, so each setting
+runs in its own process): the streamed whole-scan path gives the device
+path's stack bit for bit at any number of copy chunks, and the
+backprojector's launch shapes agree with the default to rounding."""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from tests.conftest import REPO
+
+pytestmark = pytest.mark.gpu
+
+CHILD = r"""
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, REPO)
+from ctbangbang_gb300 import lib as L, scans
+from tests import helpers as H
+out, mode = sys.argv[1], sys.argv[2]
+fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+spec = scans.tiny(1, 1, adaptive_filtration=2.0, n_slices=14, slice_thickness=2.5, seed=91)
+scan = H.Scan(spec, sys.argv[3])
+mr = scan.mr
+n_final = L.load().ctbb_n_slices_final(C.byref(mr))
+h_scan = np.ascontiguousarray(scan.frames.reshape(-1), dtype=np.float32)
+fin = np.zeros(n_final * mr.rp.nx * mr.rp.ny, np.float32)
+L.call("ctbb_reconstruct_scan_host", C.byref(mr), fp(h_scan), fp(fin), 0.0)
+np.save(out, fin)
+"""
+
+
+def run_child(tmp_path, name, env_extra):
+    out = str(tmp_path / (name + ".npy"))
+    work = tmp_path / ("w_" + name)
+    work.mkdir()
+    env = dict(os.environ, **env_extra)
+    code = "REPO = %r\n" % REPO + CHILD
+    r = subprocess.run([sys.executable, "-c", code, out, name, str(work)], env=env, capture_output=True,
+                       text=True, timeout=600, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return np.load(out)
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_streamed_path_any_chunk_count(torch_cuda, tmp_path):
+    """1, 5 and 64 copy chunks (CTBB_SCAN_CHUNKS) against the default 8: the
+    adaptive filter advances, rebin view ranges and block starts move, the
+    stack does not."""
+    want = run_child(tmp_path, "chunks8", {})
+    assert np.abs(want).max() > 0.01
+    for n in (1, 5, 64):
+        np.testing.assert_array_equal(run_child(tmp_path, "chunks%d" % n, {"CTBB_SCAN_CHUNKS": str(n)}), want)
+
+
+def test_backprojector_launch_shapes_agree(torch_cuda, tmp_path):
+    """Other CTA / warp tilings, CTA sizes and slices per thread change which
+    chunks a warp classes as flat, inner or other (whose row coordinates round
+    differently) and where slice chunks start, not the algorithm: within
+    0.01 HU of the default."""
+    want = run_child(tmp_path, "default", {})
+    hu = 1000.0 / 0.019
+    for name, env in (("w4c32", {"CTBB_BP_WARP_W": "4", "CTBB_BP_CTA_W": "32"}),
+                      ("w32", {"CTBB_BP_WARP_W": "32"}),
+                      ("t256", {"CTBB_BP_THREADS": "256", "CTBB_BP_MINB": "4"}),
+                      ("z16", {"CTBB_BP_ZPT": "16"})):
+        got = run_child(tmp_path, name, env)
+        diff = np.abs((got.astype(np.float64) - want) * hu).max()
+        print("launch shape %s: max %.2e HU from the default" % (name, diff))
+        assert diff <= 0.01, name
