@@ -147,8 +147,12 @@ def workload_sizes(mr, blocks):
         g0 = s if g0 is None else min(g0, s)
         g1 = s + ri.n_proj_pull if g1 is None else max(g1, s + ri.n_proj_pull)
     union_h2d = max(min(g1, n_readings) - max(g0, 0), 0) * frame * 4
+    n_ffs = blocks[0].n_ffs
     return dict(nht=nht, vu_per_block=vu_blocks, vu_total=sum(vu_blocks), h2d_bytes=h2d,
                 union_h2d_bytes=union_h2d,
+                union_raw_samples=(g1 - g0) * frame,
+                union_rebin_samples=((g1 - g0) // n_ffs - 2 * mr.cg.add_projections) * mr.cg.n_rows *
+                mr.cg.n_channels_oversampled,
                 raw_samples=[ri.n_proj_pull * frame for ri in blocks],
                 rebin_samples=[(ri.n_proj_pull // ri.n_ffs - 2 * mr.cg.add_projections) * mr.cg.n_rows *
                                mr.cg.n_channels_oversampled for ri in blocks])
@@ -544,10 +548,15 @@ def run_ours(args):
     traffic = read_traffic().get("backproject")
     peaks, peak_kind = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # HBM-bound stages: algorithmic bytes per launch over their measured time
-    nblk = len(blocks)
-    raw_b = sum(sizes["raw_samples"]) / nblk
-    rb_b = sum(sizes["rebin_samples"]) / nblk
+    # HBM-bound stages: algorithmic bytes per stage pass over its measured
+    # time; a pass covers the union window on the whole-scan path and one
+    # block's window on the block loop
+    if args.path == "scan":
+        raw_b, rb_b = sizes["union_raw_samples"], sizes["union_rebin_samples"]
+    else:
+        nblk = len(blocks)
+        raw_b = sum(sizes["raw_samples"]) / nblk
+        rb_b = sum(sizes["rebin_samples"]) / nblk
     stage_bytes = {"adaptive_filter": 8 * raw_b, "rebin": 4 * raw_b + 4 * rb_b, "ramp_filter": 8 * rb_b,
                    "finalize": 4 * plane * (mr.ri.n_slices_recon + n_final)}
     stages = {}
