@@ -47,6 +47,16 @@ def test_every_declared_symbol_is_exported(lib):
         assert mangled in out
 
 
+def test_integration_guide_lists_every_entry_point():
+    """The integration guide's entry-point index names every function the
+    header declares (a binding author starts from that index)."""
+    header = open(os.path.join(REPO, "include", "ctbb_gb300.h")).read()
+    declared = set(re.findall(r"^(?:const\s+)?[a-z_0-9]+\s*\*?\s*(ctbb_[a-z0-9_]+)\s*\(", header, re.M))
+    guide = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    listed = set(re.findall(r"`(ctbb_[a-z0-9_]+)`", guide))
+    assert not declared - listed, sorted(declared - listed)
+
+
 def test_version(lib):
     assert b"sm_103a" in lib.ctbb_version()
 
