@@ -442,6 +442,20 @@ extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
     return 2 * raw + rebin + image;
 }
 
+// Waits for the context's copy and compute streams when a reconstruction
+// returns, so that once a call has returned -- also one that failed halfway,
+// say on a missing filter file after its first copies were enqueued -- no
+// copy from the caller's host buffer and no kernel writing the caller's
+// output is still in flight.  After a successful call both are idle already.
+struct StreamsDrained {
+    Context &c;
+    ~StreamsDrained()
+    {
+        if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+        cudaStreamSynchronize(c.stream);
+    }
+};
+
 static int reconstruct_device_in(Context &c, struct recon_metadata *mr, const float *d_scan, float *d_final,
                                        float mu_water)
 {
@@ -453,6 +467,7 @@ static int reconstruct_device_in(Context &c, struct recon_metadata *mr, const fl
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
+    StreamsDrained drained{c};
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const size_t n_readings = (size_t)mr->rp.n_readings;
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
@@ -579,6 +594,7 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
+    StreamsDrained drained{c};
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const long long n_readings = (long long)mr->rp.n_readings;
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
@@ -951,6 +967,7 @@ static int reconstruct_scan_host_in(Context &c, struct recon_metadata *mr, const
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
+    StreamsDrained drained{c};
     HostFeed feed(h_scan, (long long)mr->rp.n_readings, mr->cg.n_rows_raw * mr->cg.n_channels);
     return scan_streamed(c, mr, feed, h_final, mu_water);
 }
@@ -1114,6 +1131,7 @@ static int reconstruct_scan_file_in(Context &c, struct recon_metadata *mr, float
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
+    StreamsDrained drained{c};
     char path[4096 + 255 + 2];
     snprintf(path, sizeof(path), "%s/%s", mr->rp.raw_data_dir, mr->rp.raw_data_file);
     FileFeed feed(path, (long long)mr->rp.raw_data_offset, mr->cg.n_rows_raw * mr->cg.n_channels);
@@ -1136,6 +1154,7 @@ static int reconstruct_host_in(Context &c, struct recon_metadata *mr, const floa
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
+    StreamsDrained drained{c};
     CTBB_TRY(ensure_copy_stream(c));
     const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
     const long long n_readings = mr->rp.n_readings;

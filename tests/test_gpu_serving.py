@@ -149,3 +149,36 @@ def test_server_refuses_a_scan_over_the_budget(torch_cuda, requests):
         with pytest.raises(L.CtbbError) as e:
             srv.submit(r.scan.mr, fptr(r.h_scan), fptr(r.h_final))
     assert e.value.status_name == "CTBB_ERR_ALLOC"
+
+
+def test_server_isolates_a_failing_request(torch_cuda, requests, tmp_path):
+    """A request that fails while it runs -- its plan names the sharp
+    reconstruction kernel, whose filter file the scan's install directory
+    lacks, so the whole-scan call fails after its first copies were enqueued
+    -- returns its error and text; the requests around it are unaffected, and
+    the failed call leaves the context usable."""
+    bad = Req(scans.tiny(0, 0, recon_kernel=3, seed=306), str(tmp_path / "bad"))
+    try:
+        want = [r.alone() for r in requests]
+        mix = requests[:2] + [bad] + requests[2:]
+        with Server(n_workers=2, device_budget_bytes=8 << 30) as srv:
+            tickets = [srv.submit(r.scan.mr, fptr(r.h_scan), fptr(r.h_final)) for r in mix]
+            results = []
+            for t in tickets:
+                try:
+                    results.append(srv.wait(t))
+                except L.CtbbError as e:
+                    results.append(e)
+        err = results[2]
+        assert isinstance(err, L.CtbbError) and err.status_name == "CTBB_ERR_IO", err
+        assert "sharp" in str(err)
+        for r, w, res in zip(requests, want, results[:2] + results[3:]):
+            assert not isinstance(res, L.CtbbError), res
+            np.testing.assert_array_equal(r.h_final, w)
+        # the same failure on the library-wide context, then a good call
+        with pytest.raises(L.CtbbError) as e:
+            bad.alone()
+        assert e.value.status_name == "CTBB_ERR_IO"
+        np.testing.assert_array_equal(requests[0].alone(), want[0])
+    finally:
+        bad.scan.close()
