@@ -41,6 +41,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
+import ctbb_synth  # noqa: E402  (synthetic scans and the FP32 peak probe)
+
 FLOP_PER_VU = 13          # q FMA 2, q_idx FMA 2, bilinear 6, s += W v 2, h += W 1
 STAGES = ["adaptive_filter", "rebin", "ramp_filter", "backproject", "finalize"]
 
@@ -224,13 +226,13 @@ def cpu_baseline(spec, mr, blocks, sizes, threads=None, steps=1, warmup=0, sub_f
     b0 = blocks[0]
     # host raw of T distinct sub-windows (generated on the CPU)
     subs = []
-    objs = scans.phantom_objects(spec)
+    objs = ctbb_synth.phantom_objects(spec)
     s0 = int(b0.idx_pull_start)
 
     def gen(t):
         start = s0 + (t * sub_frames) % max(b0.n_proj_pull - sub_frames, 1)
         start -= start % mr.ri.n_ffs
-        return scans.project_host(mr, objs, start, sub_frames, spec.i0, spec.seed)
+        return ctbb_synth.project_host(mr, objs, start, sub_frames, spec.i0, spec.seed)
 
     with cf.ThreadPoolExecutor(T) as ex:
         subs = list(ex.map(gen, range(T)))
@@ -381,13 +383,7 @@ def run_ours(args):
     n_final = lib.ctbb_n_slices_final(C.byref(mr))
 
     # synthetic scan on the device (each replica its own seed)
-    ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
-    tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
-    objs = scans.phantom_objects(spec)
-    d_scan = torch.empty(n * frame, dtype=torch.float32, device="cuda")
-    L.call("ctbb_phantom_project_device", C.byref(mr), objs, len(objs), C.c_void_p(ta.data_ptr()),
-           C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), replica_seed(spec.seed, rank),
-           C.c_void_p(d_scan.data_ptr()))
+    d_scan = ctbb_synth.project_scan_device(torch, mr, spec, seed=replica_seed(spec.seed, rank))
     d_final = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
 
     entry = {"scan": ("ctbb_reconstruct_scan_device", "ctbb_reconstruct_scan_host"),
@@ -540,7 +536,7 @@ def run_ours(args):
         return
 
     # roofline of the dominant kernel (backprojection, FP32-pipe bound)
-    peak_fp32 = lib.ctbb_fp32_peak_tflops(5)
+    peak_fp32 = ctbb_synth.fp32_peak_tflops(5, torch.cuda.current_stream().cuda_stream)
     bp_ms, bp_n = stage_ms[3], max(stage_n[3], 1)
     vu_per_launch = sizes["vu_total"] / len(blocks)
     bp_launch_ms = bp_ms / bp_n
@@ -681,15 +677,10 @@ def serve_measure(args, torch):
         prm, inst = scans.prepare(spec, wd)
         mr = scans.plan(prm, inst)
         n, frame = spec.n_readings, mr.cg.n_rows_raw * mr.cg.n_channels
-        ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
-        tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
-        objs = scans.phantom_objects(spec)
-        d = torch.empty(n * frame, dtype=torch.float32, device="cuda")
-        L.call("ctbb_phantom_project_device", C.byref(mr), objs, len(objs), C.c_void_p(ta.data_ptr()),
-               C.c_void_p(tp.data_ptr()), 0, n, C.c_float(spec.i0), spec.seed, C.c_void_p(d.data_ptr()))
+        d = ctbb_synth.project_scan_device(torch, mr, spec)
         h = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
         h.copy_(d)
-        del d, ta, tp
+        del d
         n_final = lib.ctbb_n_slices_final(C.byref(mr))
         specs.append(spec)
         prms.append((prm, inst))
@@ -791,11 +782,9 @@ def run_profile_case(args):
     nv = P // b0.n_ffs - 2 * m.cg.add_projections
     ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
     tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
-    objs = scans.phantom_objects(spec)
     d_raw = torch.empty(P * frame, dtype=torch.float32, device="cuda")
-    L.call("ctbb_phantom_project_device", C.byref(m), objs, len(objs), C.c_void_p(ta.data_ptr()),
-           C.c_void_p(tp.data_ptr()), int(b0.idx_pull_start), P, C.c_float(spec.i0), spec.seed,
-           C.c_void_p(d_raw.data_ptr()))
+    ctbb_synth.project_device(m, ctbb_synth.phantom_objects(spec), ta.data_ptr(), tp.data_ptr(), int(b0.idx_pull_start), P,
+                         spec.i0, spec.seed, d_raw.data_ptr(), torch.cuda.current_stream().cuda_stream)
     d_filt = torch.empty_like(d_raw)
     d_rb = torch.empty(nv * m.cg.n_rows * m.cg.n_channels_oversampled, dtype=torch.float32, device="cuda")
     d_blk = torch.empty(m.rp.nx * m.rp.ny * m.ri.n_slices_block, dtype=torch.float32, device="cuda")

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libctbb_gb300.so")
 
 CUDA_SOURCES = [
     "abi.cu", "adaptive_filter.cu", "rebin.cu", "ramp_filter.cu",
-    "backproject.cu", "finalize.cu", "phantom.cu", "peak_probe.cu",
+    "backproject.cu", "finalize.cu",
 ]
 HOST_SOURCES = ["planner.cpp", "dicom.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

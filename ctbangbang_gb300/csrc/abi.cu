@@ -71,7 +71,9 @@ struct Context {
     // stage work buffers
     DeviceBuffer raw_in, raw_filt, rebin, block, image, final_stack, scratch;
     // tables
-    DeviceBuffer bp_views, bp_zpos, fin_offsets, fin_slices, fin_weights;
+    DeviceBuffer bp_views, bp_theta, bp_zpos, fin_offsets, fin_slices, fin_weights;
+    // whole-scan paths: one block window filtered with its own statistics
+    DeviceBuffer edge_raw;
     DeviceRebinTables rebin_tables;
     RampFilterPlan ramp;
     void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
@@ -255,15 +257,36 @@ static int do_filter(Context &c, const struct recon_metadata &mr, float *d_rebin
     return launch_ramp_filter(c.ramp, d_rebin, d.n_views * d.n_rows, c.stream);
 }
 
-static int do_backproject(Context &c, const struct recon_metadata &mr, const float *d_rebin, float *d_block)
+// Where the rows of a block's views sit in the whole-scan paths' rows buffer:
+// view j (= i + k n_half) is row off + j of the union's rows, except views
+// [0, d0) and [d1, n_used), which were re-made from the block's own window
+// (EdgePlan) into rows patch, patch + 1, ... in that order.
+struct ViewRows {
+    size_t off = 0;
+    int d0 = 0, d1 = 0, n_used = 0;
+    size_t patch = 0;
+    unsigned row(int j) const
+    {
+        if (j < d0) return (unsigned)(patch + j);
+        if (j >= d1) return (unsigned)(patch + d0 + (j - d1));
+        return (unsigned)(off + j);
+    }
+};
+
+static int do_backproject(Context &c, const struct recon_metadata &mr, const float *d_rebin, float *d_block,
+                          const ViewRows *rows = nullptr)
 {
     BackprojectTables t;
     CTBB_TRY(build_backproject_tables(mr, &t));
+    if (rows)
+        for (int i = 0; i < t.n_half; ++i)
+            for (int k = 0; k < t.nht; ++k) t.set_view_row(i, k, rows->row(i + k * t.n_half));
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
+    CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
     CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
     StageScope scope(c, 3);
-    return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_zpos.as<float>(), d_rebin, d_block,
-                              bp_zpt(), c.stream);
+    return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
+                              d_rebin, d_block, bp_zpt(), c.stream);
 }
 
 static int do_finalize(Context &c, const struct recon_metadata &mr, const float *d_image, float *d_final, float mu_water)
@@ -314,7 +337,8 @@ static void release_context(Context &c, bool device_sync, bool unbind)
         }
     }
     for (DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
-                            &c.scratch, &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices, &c.fin_weights})
+                            &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
+                            &c.fin_weights, &c.edge_raw})
         b->release();
     if (c.rebin_tables.base) cudaFree(c.rebin_tables.base);
     c.rebin_tables = DeviceRebinTables{};
@@ -550,6 +574,99 @@ static int plan_union(struct recon_metadata *mr, std::vector<struct recon_info> 
     return CTBB_OK;
 }
 
+// first rebinned view of block b in the union's rebinned rows
+static size_t union_view_offset(const struct recon_info &ri, long long g0)
+{
+    return (size_t)(((long long)(int)ri.idx_pull_start - g0) / (long long)ri.n_ffs);
+}
+
+// Views of one block that the whole-scan paths re-make from the block's own
+// pull window.  The reference filters every block's window on its own
+// (src/main.cu:222, the window of src/setup.cu:637-661), and the adaptive
+// filter's 18- and 180-degree statistics (include/preprocessing.cuh:87-206)
+// stop at that window's ends.  Within adaptive_filter_edge_reach frames of a
+// window end that is not also an end of the union window, the block's
+// filtered frames can therefore differ from the union's; elsewhere they are
+// the same.  The block's views [0, d0) and [d1, n_used) read such frames
+// (rebin_frames_needed bounds a view's frames from above; a view j reads no
+// frame below n_ffs (j - 2)); they are rebinned from frames [0, fa) and
+// [fb, P) of the block's window filtered with the block's own thresholds.
+struct EdgePlan {
+    int d0 = 0, d1 = 0, n_used = 0, fa = 0, fb = 0;
+    bool any() const { return d0 > 0 || d1 < n_used; }
+    int n_patch() const { return d0 + (n_used - d1); }
+};
+
+static EdgePlan edge_plan(const struct recon_metadata &mb, long long g0, long long g1)
+{
+    EdgePlan e;
+    BlockDims d = block_dims(mb);
+    const long long P = (long long)d.n_proj_pull, n_ffs = (long long)d.n_ffs;
+    const long long add = (long long)mb.cg.add_projections;
+    const long long s = (long long)(int)mb.ri.idx_pull_start;
+    const long long reach = adaptive_filter_edge_reach(mb);
+    e.n_used = d.n_half_turns * (int)(mb.cg.n_proj_turn / 2);
+    e.d1 = e.n_used;
+    if (s > g0) e.d0 = (int)std::min<long long>(e.n_used, (reach + n_ffs - 1) / n_ffs + 2);
+    if (s + P < g1) {
+        long long last_clean = (P - reach) >= 0 ? (P - reach) / n_ffs - 2 * add - 2 : -1;
+        e.d1 = (int)std::max<long long>(e.d0, std::min<long long>(e.n_used, last_clean + 1));
+    }
+    e.fa = e.d0 > 0 ? (int)std::min(P, n_ffs * (e.d0 - 1 + 2 * add + 2)) : 0;
+    e.fb = e.d1 < e.n_used ? (int)std::max(0LL, n_ffs * (e.d1 - 2)) : (int)P;
+    if (e.fb < e.fa) e.fb = e.fa;
+    return e;
+}
+
+// Largest pull window and edge patch (views) over the blocks of a plan.
+static void edge_extent(const struct recon_metadata &mr, const std::vector<struct recon_info> &blocks,
+                        long long g0, long long g1, size_t *max_pull, size_t *max_patch)
+{
+    *max_pull = 0;
+    *max_patch = 0;
+    for (const auto &ri : blocks) {
+        struct recon_metadata mb = mr;
+        mb.ri = ri;
+        EdgePlan e = edge_plan(mb, g0, g1);
+        *max_pull = std::max(*max_pull, (size_t)ri.n_proj_pull);
+        *max_patch = std::max(*max_patch, (size_t)e.n_patch());
+    }
+}
+
+// Re-makes the edge views of block mb: its window's thresholds from its own
+// statistics (the frames' maxima are the union's, d_union_sup at the block's
+// offset), frames [0, fa) and [fb, P) of the window filtered into c.edge_raw,
+// the block's views [0, d0) and [d1, n_used) rebinned from there with the
+// block's own view-axis coordinates (the tables are the union's; only the
+// window length differs) into d_patch, and ramp-filtered.
+static int run_edge_patch(Context &c, const struct recon_metadata &mb, const EdgePlan &e, const RebinTables &rt,
+                          const float *d_union_raw, const float *d_union_sup, long long g0, float *d_block_scratch,
+                          float *d_patch)
+{
+    BlockDims d = block_dims(mb);
+    const size_t frame = d.n_rows_raw * d.n_channels;
+    const size_t view_elems = d.n_rows * d.n_os;
+    const long long sb = (long long)(int)mb.ri.idx_pull_start - g0;
+    {
+        StageScope scope(c, 0);
+        CTBB_TRY(launch_adaptive_filter_ends(mb, d_union_raw + (size_t)sb * frame, c.edge_raw.as<float>(),
+                                             d_union_sup + sb, d_block_scratch, e.fa, e.fb, c.stream));
+    }
+    RebinTables tb = rt;
+    tb.split_view_coord = 0;  // the block's own float coordinates, as its block loop
+    tb.n_proj = (int)(d.n_proj_pull / d.n_ffs);
+    tb.n_views = tb.n_proj - 2 * tb.add_projections;
+    {
+        StageScope scope(c, 1);
+        if (e.d0 > 0) CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(), d_patch, c.stream, 0, e.d0));
+        if (e.d1 < e.n_used)
+            CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(),
+                                  d_patch - (size_t)(e.d1 - e.d0) * view_elems, c.stream, e.d1, e.n_used));
+    }
+    StageScope scope(c, 2);
+    return launch_ramp_filter(c.ramp, d_patch, (size_t)e.n_patch() * d.n_rows, c.stream);
+}
+
 // Device bytes the whole-scan paths (scan_device / scan_host / scan_file)
 // hold for this plan: the union window raw and filtered, its rebinned rows,
 // the adaptive filter's statistics, the image and final stacks, plus 8 MiB
@@ -565,16 +682,15 @@ extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
     BlockDims dg = block_dims(mg);
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     const int n_final = ctbb_n_slices_final(mr);
-    return (2 * dg.raw_elems() + dg.rebin_elems() + adaptive_filter_scratch_floats(dg.n_proj_pull) +
+    size_t max_pull = 0, max_patch = 0;
+    edge_extent(m, blocks, g0, g1, &max_pull, &max_patch);
+    const size_t frame = dg.n_rows_raw * dg.n_channels, view_elems = dg.n_rows * dg.n_os;
+    return (2 * dg.raw_elems() + dg.rebin_elems() + max_patch * view_elems + max_pull * frame +
+            adaptive_filter_scratch_floats(dg.n_proj_pull) + adaptive_filter_scratch_floats(max_pull) +
             plane * mr->ri.n_slices_recon + plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
            ((size_t)8 << 20);
 }
 
-// first rebinned view of block b in the union's rebinned rows
-static size_t union_view_offset(const struct recon_info &ri, long long g0)
-{
-    return (size_t)(((long long)(int)ri.idx_pull_start - g0) / (long long)ri.n_ffs);
-}
 
 // Whole scan with one resident rebinned scan: the union of all blocks' pull
 // windows is adaptive-filtered, rebinned and ramp-filtered once, and every
@@ -619,17 +735,42 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
     }
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    CTBB_TRY(do_adaptive(c, mg, d_win, c.raw_filt.as<float>()));
-    CTBB_TRY(c.rebin.ensure(dg.rebin_elems() * sizeof(float)));
-    CTBB_TRY(do_rebin(c, mg, c.raw_filt.as<float>(), c.rebin.as<float>()));
-    CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
+    size_t max_pull = 0, max_patch = 0;
+    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
+    const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
+    CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
+    {
+        StageScope scope(c, 0);
+        CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
+    }
     const size_t view_elems = dg.n_rows * dg.n_os;
+    CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * view_elems) * sizeof(float)));
+    RebinTables rt;
+    CTBB_TRY(build_rebin_tables(mg, &rt));
+    rt.split_view_coord = 1;  // the union's frame offsets are large
+    CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
+    {
+        StageScope scope(c, 1);
+        CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
+    }
+    CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
+    if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
     for (size_t b = 0; b < blocks.size(); ++b) {
         mr->ri = blocks[b];
-        // view j of block b is view j + (pull_start_b - g0) / n_ffs of the union
-        size_t off = union_view_offset(blocks[b], g0);
+        // view j of block b is view j + (pull_start_b - g0) / n_ffs of the
+        // union, except its edge views, re-made after the union's rows
+        ViewRows vr;
+        vr.off = union_view_offset(blocks[b], g0);
+        EdgePlan e = edge_plan(*mr, g0, g1);
+        vr.d0 = e.d0;
+        vr.d1 = e.d1;
+        vr.n_used = e.n_used;
+        vr.patch = dg.n_views;
+        if (e.any())
+            CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
+                                    c.rebin.as<float>() + dg.n_views * view_elems));
         float *slab = c.image.as<float>() + b * n_block * plane;
-        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>() + off * view_elems, slab));
+        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr));
     }
     CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
@@ -855,10 +996,14 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     BlockDims dg = block_dims(mg);
     const int G = (int)(g1 - g0);
     int n_final = ctbb_n_slices_final(mr);
+    size_t max_pull = 0, max_patch = 0;
+    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
+    const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
     CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    CTBB_TRY(c.rebin.ensure(dg.rebin_elems() * sizeof(float)));
-    CTBB_TRY(c.scratch.ensure(adaptive_filter_scratch_floats(dg.n_proj_pull) * sizeof(float)));
+    CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * dg.n_rows * dg.n_os) * sizeof(float)));
+    CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
+    if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
     CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
     // the union window in chunks of whole focal-spot cycles; the copy stream
@@ -880,6 +1025,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     RebinTables rt;
     std::vector<float> taps(2 * dg.n_os);
     if (status == CTBB_OK) status = build_rebin_tables(mg, &rt);
+    rt.split_view_coord = 1;  // the union's frame offsets are large
     if (status == CTBB_OK) status = upload_rebin_tables(rt, &c.rebin_tables, c.stream);
     if (status == CTBB_OK) status = ctbb_load_filter(&mg, taps.data());
     if (status == CTBB_OK) status = prepare_ramp_filter(taps.data(), (int)dg.n_os, &c.ramp, c.stream);
@@ -923,7 +1069,8 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             if (status != CTBB_OK) break;
             v_done = v_ready;
         }
-        // blocks whose views (i + k n_half, k < nht) are all ready
+        // blocks whose views (i + k n_half, k < nht) are all ready, and, for a
+        // block with edge views, whose whole window has arrived
         while (b_done < blocks.size() && status == CTBB_OK) {
             struct recon_metadata mb = *mr;
             mb.ri = blocks[b_done];
@@ -931,10 +1078,22 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             size_t need = union_view_offset(blocks[b_done], g0) +
                           (size_t)db.n_half_turns * (size_t)(mr->cg.n_proj_turn / 2);
             if (need > (size_t)v_done && v_done < V) break;
+            EdgePlan e = edge_plan(mb, g0, g1);
+            const long long sb = (long long)(int)blocks[b_done].idx_pull_start - g0;
+            if (e.any() && af.n_sup < sb + (long long)db.n_proj_pull) break;
             mr->ri = blocks[b_done];
+            ViewRows vr;
+            vr.off = union_view_offset(blocks[b_done], g0);
+            vr.d0 = e.d0;
+            vr.d1 = e.d1;
+            vr.n_used = e.n_used;
+            vr.patch = dg.n_views;
+            if (e.any())
+                status = run_edge_patch(c, mb, e, rt, d_raw, c.scratch.as<float>(), g0,
+                                        c.scratch.as<float>() + af_union, c.rebin.as<float>() + dg.n_views * view_elems);
+            if (status != CTBB_OK) break;
             float *slab = c.image.as<float>() + b_done * n_block * plane;
-            status = do_backproject(c, *mr, c.rebin.as<float>() + union_view_offset(blocks[b_done], g0) * view_elems,
-                                    slab);
+            status = do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr);
             ++b_done;
         }
     }
@@ -1265,8 +1424,8 @@ static size_t context_device_bytes(const Context &c)
 {
     size_t n = 0;
     for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
-                                  &c.scratch, &c.bp_views, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                                  &c.fin_weights})
+                                  &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
+                                  &c.fin_weights, &c.edge_raw})
         n += b->bytes;
     return n + c.ramp.capacity * sizeof(float2);
 }

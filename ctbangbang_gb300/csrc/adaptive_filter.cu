@@ -410,6 +410,26 @@ int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, f
     return af_launch(p, 0, p.P, 0, p.P, 0, p.P, stream);
 }
 
+int adaptive_filter_edge_reach(const struct recon_metadata &mr)
+{
+    AfParams p;
+    float dummy = 0.0f;
+    if (af_params(mr, &dummy, &dummy, &dummy, &p) != CTBB_OK) return 0;
+    return p.range_offset + p.avg_offset;
+}
+
+int launch_adaptive_filter_ends(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                                const float *d_sup, float *d_scratch, int fa, int fb, cudaStream_t stream)
+{
+    AfParams p;
+    CTBB_TRY(af_params(mr, d_in, d_out, d_scratch, &p));
+    p.sup = const_cast<float *>(d_sup);  // read only: no maxima are launched
+    fa = std::min(std::max(fa, 0), p.P);
+    fb = std::min(std::max(fb, fa), p.P);
+    CTBB_TRY(af_launch(p, 0, 0, 0, p.P, 0, fa, stream));
+    return af_launch(p, 0, 0, 0, 0, fb, p.P, stream);
+}
+
 AfStream::AfStream(const struct recon_metadata &mr) : P((int)mr.ri.n_proj_pull)
 {
     int n_proj_ffs = (int)mr.cg.n_proj_ffs;

@@ -15,6 +15,21 @@ size_t adaptive_filter_scratch_floats(size_t n_proj_pull);
 int launch_adaptive_filter(const struct recon_metadata &mr, const float *d_in, float *d_out,
                            float *d_scratch, cudaStream_t stream);
 
+// Frames from either end of a pull window within which the filter's output
+// depends on where the window ends: the 180-degree statistics window of a
+// frame reaches range_offset frames, and each moving mean in it a further
+// avg_offset (include/preprocessing.cuh:92-96, :119-122).  Frames at least
+// this far from both ends are filtered the same in any window holding them.
+int adaptive_filter_edge_reach(const struct recon_metadata &mr);
+
+// The filter of one pull window whose per-frame maxima are given (d_sup, P
+// floats: the maxima of a larger window at this window's offset -- a frame's
+// maximum does not depend on the window): moving means of every frame, then
+// thresholds and output of frames [0, fa) and [fb, P) only.  d_scratch holds
+// 6 * P floats (the sup slot is not used).
+int launch_adaptive_filter_ends(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                                const float *d_sup, float *d_scratch, int fa, int fb, cudaStream_t stream);
+
 // The same filter over a window whose frames arrive in order: advance() is
 // told how many leading frames of d_in are present and launches every step
 // for the frames whose windows those cover (maxima as frames arrive; moving

@@ -52,7 +52,8 @@ struct BpParams {
     const float *rebin;    // [V][R][Nos]
     uint64_t rebin_rows;   // address of rebin - kFloorMagicBits rows (mod 2^64): see row_floor
     float *out;            // [n_slices_block][ny][nx]
-    const float4 *views;   // [n_half][nht] {theta, sin, cos, theta z_rot / 2 pi'}
+    const float4 *views;   // [n_half][nht] {row index bits, sin, cos, theta z_rot / 2 pi'}
+    const float *theta;    // [n_half][nht] theta (the last-turn border recheck)
     const float *zpos;     // [n_slices_block]
     int nx, ny, n_slices, nos, n_rows, nht, n_half;
     float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
             const uint64_t view_rows =
-                p.rebin_rows + ((uint64_t)(unsigned)(i + k * p.n_half) * view_stride + (unsigned)ip) * sizeof(float);
+                p.rebin_rows + ((uint64_t)__float_as_uint(t.x) * view_stride + (unsigned)ip) * sizeof(float);
             // Slices are processed in pairs (z, z + 1) with packed FP32
             // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
             // conversions and loads stay per slice.
@@ -382,14 +383,15 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                             float d = ql.x - q_max_last;
                             if (d > kBorderBand) ok_x = false;
                             else if (d > -kBorderBand)
-                                ok_x = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat, __ldg(p.zpos + z0 + 2 * m), k);
+                                ok_x = last_turn_sample_valid(p, x, y, __ldg(p.theta + (size_t)i * p.nht + k), t.y,
+                                                              t.z, phat, __ldg(p.zpos + z0 + 2 * m), k);
                         }
                         if (ok_y) {
                             float d = ql.y - q_max_last;
                             if (d > kBorderBand) ok_y = false;
                             else if (d > -kBorderBand)
-                                ok_y = last_turn_sample_valid(p, x, y, t.x, t.y, t.z, phat,
-                                                              __ldg(p.zpos + z0 + 2 * m + 1), k);
+                                ok_y = last_turn_sample_valid(p, x, y, __ldg(p.theta + (size_t)i * p.nht + k), t.y,
+                                                              t.z, phat, __ldg(p.zpos + z0 + 2 * m + 1), k);
                         }
                         s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
                     }
@@ -496,12 +498,14 @@ int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables 
     t->n_half = (int)(cg.n_proj_turn / 2);
     t->n_slices = (int)mr.ri.n_slices_block;
     t->views.resize((size_t)t->n_half * t->nht * 4);
+    t->theta.resize((size_t)t->n_half * t->nht);
     for (int i = 0; i < t->n_half; ++i)
         for (int k = 0; k < t->nht; ++k) {
             // src/backproject_cpu.cu:102-103
             float theta = t->tube_start + (2.0f * pi / (float)cg.n_proj_turn) * (float)i + (float)k * pi;
             float *v = &t->views[((size_t)i * t->nht + k) * 4];
-            v[0] = theta;
+            t->set_view_row(i, k, (unsigned)(i + k * t->n_half));
+            t->theta[(size_t)i * t->nht + k] = theta;
             v[1] = std::sin(theta);
             v[2] = std::cos(theta);
             v[3] = theta * (cg.z_rot / (2.0f * pi));  // theta z_rot / 2 pi': the ray's table term
@@ -513,8 +517,14 @@ int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables 
     return CTBB_OK;
 }
 
+void BackprojectTables::set_view_row(int i, int k, unsigned row)
+{
+    uint32_t bits = row;
+    std::memcpy(&views[((size_t)i * nht + k) * 4], &bits, sizeof(bits));
+}
+
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
-                       const float4 *d_views, const float *d_zpos, const float *d_rebin,
+                       const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
                        float *d_block, int zpt, cudaStream_t stream)
 {
     const struct ct_geom &cg = mr.cg;
@@ -528,6 +538,7 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
                    (uint64_t)kFloorMagicBits * (uint64_t)cg.n_channels_oversampled * sizeof(float);
     p.out = d_block;
     p.views = d_views;
+    p.theta = d_theta;
     p.zpos = d_zpos;
     p.nx = (int)rp.nx;
     p.ny = (int)rp.ny;

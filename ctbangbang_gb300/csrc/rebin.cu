@@ -229,6 +229,7 @@ struct RebinParams {
     const FocalTerm *focal;     // mode dependent
     float focal_offset[4];
     int n_ffs, N, Nos, R_raw, R, n_proj, add, n_views, reverse_rows;
+    int split_view_coord;
     int v_begin, v_end;  // views this launch writes
 };
 
@@ -251,6 +252,52 @@ __device__ __forceinline__ void view_taps(float a, int n, int *i0, int *i1, floa
     *w = __fsub_rn(a, fl);
     *i0 = (int)fl;
     *i1 = (a == (float)n - 1.0f) ? *i0 : *i0 + 1;
+}
+
+// The same taps from the coordinate ((n_ffs proj - t_alpha) - t_off - q) /
+// n_ffs evaluated in split form.  In float that expression rounds at the
+// magnitude of n_ffs proj: within one block's pull window (proj below ~2500)
+// to 5e-4 frames, but in the whole-scan union (proj up to ~11000 at 40
+// turns) to 4e-3 frames, which moves the view weights of the later blocks by
+// up to 1e-3.  Here c = t_alpha + t_off + q (a few hundred frames) is split
+// into floor(c) and the exact remainder c - floor(c); n_ffs proj - floor(c)
+// is an exact integer J = n_ffs Q + m with 0 <= m < n_ffs, and the coordinate
+// is Q + (m - (c - floor(c))) / n_ffs, whose fraction is rounded at a
+// magnitude below n_ffs.  The result differs from the exact coordinate by
+// about 1e-7 views, from any block's own float coordinate by at most that
+// block's rounding.  Same clamp and edge alias as view_taps.
+__device__ __forceinline__ void view_taps_split(int n_ffs, int proj, float t_alpha, float t_off, int q, int n,
+                                                int *i0, int *i1, float *w)
+{
+    float c = __fadd_rn(__fadd_rn(t_alpha, t_off), (float)q);
+    float cf = floorf(c);
+    float c_frac = __fsub_rn(c, cf);  // exact: same binade or finer
+    int J = n_ffs * proj - (int)cf;
+    int Q = J >= 0 ? J / n_ffs : -((-J + n_ffs - 1) / n_ffs);
+    int m = J - Q * n_ffs;
+    float r = __fsub_rn((float)m, c_frac);  // in (-1, n_ffs)
+    r = n_ffs == 1 ? r : __fmul_rn(r, n_ffs == 2 ? 0.5f : 0.25f);
+    if (r < 0.0f) {  // floor
+        Q -= 1;
+        r = __fadd_rn(r, 1.0f);
+        if (r >= 1.0f) {  // -r rounded to below 1 ulp of 1
+            Q += 1;
+            r = 0.0f;
+        }
+    }
+    if (Q < 0) {
+        *i0 = 0;
+        *i1 = n > 1 ? 1 : 0;
+        *w = 0.0f;
+    } else if (Q > n - 1 || (Q == n - 1 && r > 0.0f)) {
+        *i0 = n - 1;
+        *i1 = n - 1;
+        *w = 0.0f;
+    } else {
+        *i0 = Q;
+        *i1 = (Q == n - 1) ? Q : Q + 1;
+        *w = r;
+    }
 }
 
 // Views per thread: the per-channel taps and focal terms are loaded once and
@@ -287,10 +334,12 @@ __global__ void rebin_bilinear_kernel(RebinParams p)
         const float omu = tap.one_minus_u, u = tap.u;
         const float *base = p.raw + s * frame_stride;
         for (int v = v0; v < min(v0 + kViewsPerThread, p.v_end); ++v) {
-            float alpha = focal_alpha(p.n_ffs, v + p.add, t_alpha, t_off, s);
             int i0, i1;
             float w;
-            view_taps(alpha, p.n_proj, &i0, &i1, &w);
+            if (p.split_view_coord)
+                view_taps_split(p.n_ffs, v + p.add, t_alpha, t_off, s, p.n_proj, &i0, &i1, &w);
+            else
+                view_taps(focal_alpha(p.n_ffs, v + p.add, t_alpha, t_off, s), p.n_proj, &i0, &i1, &w);
             const float *f0 = base + (Idx)(p.n_ffs * i0) * frame_stride;
             const float *f1 = base + (Idx)(p.n_ffs * i1) * frame_stride;
             float omw = __fsub_rn(1.0f, w);
@@ -340,8 +389,13 @@ __global__ void rebin_two_stage_kernel(RebinParams p)
             int proj = v + p.add;
             int i0, i1, j0, j1;
             float w0, w1;
-            view_taps(focal_alpha(p.n_ffs, proj, ta0, to0, q0), p.n_proj, &i0, &i1, &w0);
-            view_taps(focal_alpha(p.n_ffs, proj, ta1, to1, q1), p.n_proj, &j0, &j1, &w1);
+            if (p.split_view_coord) {
+                view_taps_split(p.n_ffs, proj, ta0, to0, q0, p.n_proj, &i0, &i1, &w0);
+                view_taps_split(p.n_ffs, proj, ta1, to1, q1, p.n_proj, &j0, &j1, &w1);
+            } else {
+                view_taps(focal_alpha(p.n_ffs, proj, ta0, to0, q0), p.n_proj, &i0, &i1, &w0);
+                view_taps(focal_alpha(p.n_ffs, proj, ta1, to1, q1), p.n_proj, &j0, &j1, &w1);
+            }
             const float *f00 = b0 + (Idx)(p.n_ffs * i0) * frame_stride;
             const float *f01 = b0 + (Idx)(p.n_ffs * i1) * frame_stride;
             const float *f10 = b1 + (Idx)(p.n_ffs * j0) * frame_stride;
@@ -391,6 +445,7 @@ int launch_rebin(const RebinTables &t, const DeviceRebinTables &dt, const float 
     p.add = t.add_projections;
     p.n_views = t.n_views;
     p.reverse_rows = t.reverse_rows;
+    p.split_view_coord = t.split_view_coord;
     p.v_begin = v_begin;
     p.v_end = v_end;
     int chunks = (v_end - v_begin + kViewsPerThread - 1) / kViewsPerThread;

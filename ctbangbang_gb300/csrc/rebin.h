@@ -26,6 +26,11 @@ struct RebinTables {
     RebinMode mode = RebinMode::kNoFfs;
     int n_ffs = 1, n_channels = 0, n_os = 0, n_rows_raw = 0, n_rows = 0;
     int n_proj = 0, add_projections = 0, n_views = 0, reverse_rows = 0;
+    // View-axis coordinate in split form (integer frames + a fraction) instead
+    // of the reference's float expression: for a window far longer than one
+    // block's (the whole-scan union), where that float rounds at the
+    // window's large frame offsets (rebin.cu, view_taps_split).
+    int split_view_coord = 0;
     std::vector<AxisTap> out_taps;   // [side][n_os]
     std::vector<FocalTerm> focal;    // no/z-FFS: [side][n_os]; phi/both: [focal][n_channels]
     std::vector<float> focal_offset; // d_alpha_r * n_proj_ffs / (2 pi) per focal spot

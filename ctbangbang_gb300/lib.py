@@ -8,7 +8,7 @@ CTBB_ERR_NO_DEVICE when no CUDA device is present.
 import ctypes as C
 import os
 
-from .structs import PhantomObject, ReconMetadata, ReconParams
+from .structs import ReconMetadata, ReconParams
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libctbb_gb300.so")
 
@@ -70,15 +70,10 @@ PROTOTYPES = {
     "ctbb_reconstruct_host": (C.c_int, [_MR, _F, _F, C.c_float]),
     "ctbb_profile_enable": (C.c_int, [C.c_int]),
     "ctbb_profile_read": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int, C.c_int]),
-    "ctbb_fp32_peak_tflops": (C.c_double, [C.c_int]),
     "ctbb_workspace_bytes": (C.c_size_t, [_MR]),
     "ctbb_release_workspace": (C.c_int, []),
     "ctbb_kernel_launch_count": (C.c_uint64, []),
     "ctbb_struct_layout": (C.c_int, [C.POINTER(C.c_size_t), C.c_int]),
-    "ctbb_phantom_project_host": (C.c_int, [_MR, C.POINTER(PhantomObject), C.c_int, C.c_size_t,
-                                            C.c_size_t, C.c_float, C.c_uint64, _F]),
-    "ctbb_phantom_project_device": (C.c_int, [_MR, C.POINTER(PhantomObject), C.c_int, _VP, _VP,
-                                              C.c_size_t, C.c_size_t, C.c_float, C.c_uint64, _VP]),
 }
 
 

@@ -1,9 +1,9 @@
 """Scan descriptions, .prm / .scanner writers, planning and seeded phantoms.
 
 The reference ships no raw data, so every workload here is a seeded synthetic
-helical scan: a water cylinder (r = 150 mm, mu = 0.019/mm) plus random
-ellipsoids (semi-axes 5-60 mm, mu 0.015-0.04/mm, random orientation), analytic
-line integrals and Poisson noise, generated by the library's phantom projector.
+helical scan (water cylinder plus random ellipsoids) whose frames the test and
+benchmark generator (the synth package) projects; this module only describes
+the scans and plans them through the library.
 
 Named workloads (sizes of the benchmark configurations):
   config1  672 ch x 16 rows (1.2 mm), 1152 views/turn, pitch 1.0, 3 turns,
@@ -23,7 +23,7 @@ import os
 import numpy as np
 
 from . import lib as _lib
-from .structs import PhantomObject, ReconMetadata, ReconParams
+from .structs import ReconMetadata, ReconParams
 
 MU_WATER = 0.019
 
@@ -269,56 +269,6 @@ def free_plan(mr):
     """Frees the host arrays of a plan (ctbb_finish_and_cleanup without the file)."""
     mr.ctd.final_image_stack = None
     _lib.call("ctbb_finish_and_cleanup", C.byref(mr))
-
-
-# --------------------------------------------------------------------------
-# phantom
-# --------------------------------------------------------------------------
-
-def _rotation(rng):
-    q = rng.normal(size=4)
-    q /= np.linalg.norm(q)
-    w, x, y, z = q
-    return np.array([
-        [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
-        [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
-        [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)],
-    ])
-
-
-def phantom_objects(spec, z_range=None):
-    """Water cylinder + spec.n_ellipsoids seeded random ellipsoids (mu values
-    absolute inside each ellipsoid, stored as differences to water)."""
-    rng = np.random.default_rng(spec.seed)
-    if z_range is None:
-        z_range = (spec.start_pos - 5 * spec.slice_thickness, spec.end_pos + 5 * spec.slice_thickness)
-    objs = (PhantomObject * (1 + spec.n_ellipsoids))()
-    cyl = objs[0]
-    cyl.kind = 0
-    cyl.mu = MU_WATER
-    cyl.semi_axes[0] = spec.cylinder_radius
-    r_max = spec.cylinder_radius
-    lo, hi = spec.semi_axis_range
-    for i in range(spec.n_ellipsoids):
-        o = objs[1 + i]
-        o.kind = 1
-        axes = rng.uniform(lo, hi, size=3)
-        rad = rng.uniform(0, max(r_max - axes.max(), 0.0) * 0.9)
-        ang = rng.uniform(0, 2 * math.pi)
-        zc = rng.uniform(*z_range)
-        o.center[:] = [rad * math.cos(ang), rad * math.sin(ang), zc]
-        o.semi_axes[:] = list(axes)
-        o.rotation[:] = list(_rotation(rng).ravel())
-        o.mu = rng.uniform(*spec.mu_range) - MU_WATER
-    return objs
-
-
-def project_host(mr, objs, frame0, n_frames, i0, seed):
-    """Host forward projection of frames [frame0, frame0+n_frames)."""
-    out = np.empty((n_frames, mr.cg.n_rows_raw, mr.cg.n_channels), dtype=np.float32)
-    _lib.call("ctbb_phantom_project_host", C.byref(mr), objs, len(objs), frame0, n_frames,
-              C.c_float(i0), seed, out.ctypes.data_as(C.POINTER(C.c_float)))
-    return out
 
 
 def write_raw(path, frames):

@@ -9,7 +9,7 @@ import ctypes as C
 
 __all__ = [
     "ReconParams", "BlockInfo", "ReconInfo", "CtData", "CtGeom", "Flags",
-    "ReconMetadata", "PhantomObject",
+    "ReconMetadata",
 ]
 
 
@@ -141,17 +141,6 @@ class ReconMetadata(C.Structure):
         ("ctd", CtData),
         ("tube_angles", C.POINTER(C.c_float)),
         ("table_positions", C.POINTER(C.c_double)),
-    ]
-
-
-class PhantomObject(C.Structure):
-    """struct ctbb_phantom_object: kind 0 = infinite z-cylinder, 1 = ellipsoid."""
-    _fields_ = [
-        ("kind", C.c_int),
-        ("mu", C.c_float),
-        ("center", C.c_float * 3),
-        ("semi_axes", C.c_float * 3),
-        ("rotation", C.c_float * 9),
     ]
 
 

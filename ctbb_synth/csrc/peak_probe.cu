@@ -1,15 +1,18 @@
 // peak_probe.cu -- FP32 FMA throughput of the device, measured.
 //
 // The backprojector is bound by the FP32 pipe; its roofline needs the FP32
-// peak of this GPU under the clocks of the run.  Each thread runs 16
+// peak of this GPU under the clocks of the run (the measured peaks of the
+// pool hold HBM and BF16 figures only).  Measurement infrastructure, built
+// into libctbb_synth.so, not into the reconstruction library.  Each thread runs 16
 // independent FMA chains (enough to hide the FMA latency) for a fixed number
 // of iterations on registers only; the result is stored so the work is kept.
 #include <cuda_runtime.h>
 
-#include "ctbb_internal.h"
-#include "cuda_util.cuh"
+#include <algorithm>
 
-namespace ctbb {
+#include "synth.h"
+
+namespace synth {
 namespace {
 
 constexpr int kChains = 16;
@@ -31,18 +34,21 @@ __global__ void __launch_bounds__(256) ffma_probe_kernel(float *out, float a, fl
 }
 
 }  // namespace
-}  // namespace ctbb
+}  // namespace synth
 
-using namespace ctbb;
+using namespace synth;
 
 // Best of `repeats` launches, in TFLOP/s (2 FLOP per FMA).
-extern "C" double ctbb_fp32_peak_tflops(int repeats)
+extern "C" double synth_fp32_peak_tflops(int repeats, void *stream)
 {
-    if (require_device()) return -1.0;
-    cudaStream_t s = current_stream();
+    int n_dev = 0, dev = 0, sms = 0;
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev == 0) return -1.0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1.0;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     float *d = nullptr;
     if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) return -1.0;
-    int blocks = num_sms() * 8;
+    int blocks = sms * 8;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -57,7 +63,6 @@ extern "C" double ctbb_fp32_peak_tflops(int repeats)
         double flop = 2.0 * kChains * (double)kIters * blocks * 256.0;
         if (r > 0 && ms > 0) best = std::max(best, flop / (ms * 1e-3) / 1e12);
     }
-    count_launch(repeats + 1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d);

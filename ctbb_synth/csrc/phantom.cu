@@ -1,7 +1,8 @@
 // phantom.cu -- analytic forward projector for seeded helical phantoms.
 //
 // Produces the raw input of the hot path (test and benchmark data; the
-// reference ships no raw data).  The geometry is the one the reference's
+// reference ships no raw data).  Test infrastructure: built into
+// libctbb_synth.so, not into the reconstruction library.  The geometry is the one the reference's
 // rebinning and backprojection invert:
 //
 //  * frame f: nominal source angle phi_f = tube_angles[f] (deg) and source z =
@@ -24,14 +25,28 @@
 // range and the host/device variants agree up to libm rounding.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdarg>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
-#include "ctbb_internal.h"
-#include "cuda_util.cuh"
+#include "synth.h"
 
-namespace ctbb {
+namespace synth {
+
+namespace {
+thread_local char g_error[512] = "";
+}
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_error, sizeof(g_error), fmt, ap);
+    va_end(ap);
+}
 
 constexpr int kMaxPhantomObjects = 128;
 
@@ -194,7 +209,7 @@ static int make_scan(const struct recon_metadata *mr, const ctbb_phantom_object 
 {
     if (!mr || (!objects && n_objects) || n_objects < 0 || n_objects > kMaxPhantomObjects) {
         set_error("phantom: bad arguments (at most %d objects)", kMaxPhantomObjects);
-        return CTBB_ERR_ARGUMENT;
+        return 1;
     }
     const struct ct_geom &cg = mr->cg;
     memset(s, 0, sizeof(*s));
@@ -218,21 +233,22 @@ static int make_scan(const struct recon_metadata *mr, const ctbb_phantom_object 
     if (n_objects) memcpy(s->obj, objects, sizeof(ctbb_phantom_object) * (size_t)n_objects);
     if (s->n_channels <= 0 || s->n_rows_raw <= 0) {
         set_error("phantom: geometry not configured");
-        return CTBB_ERR_STATE;
+        return 8;
     }
-    return CTBB_OK;
+    return 0;
 }
 
-}  // namespace ctbb
+}  // namespace synth
 
-using namespace ctbb;
+using namespace synth;
 
-extern "C" int ctbb_phantom_project_host(const struct recon_metadata *mr,
-                                         const struct ctbb_phantom_object *objects, int n_objects,
-                                         size_t frame0, size_t n_frames, float i0, uint64_t seed,
-                                         float *out)
+extern "C" const char *synth_last_error(void) { return g_error; }
+
+extern "C" int synth_project_host(const struct recon_metadata *mr, const struct ctbb_phantom_object *objects,
+                                  int n_objects, size_t frame0, size_t n_frames, float i0, uint64_t seed,
+                                  float *out)
 {
-    clear_error();
+    g_error[0] = 0;
     PhantomScan *s = new PhantomScan;
     int st = make_scan(mr, objects, n_objects, i0, seed, s);
     if (st) {
@@ -242,7 +258,7 @@ extern "C" int ctbb_phantom_project_host(const struct recon_metadata *mr,
     if (!out || !mr->tube_angles || !mr->table_positions) {
         delete s;
         set_error("phantom: null output or frame tables");
-        return CTBB_ERR_ARGUMENT;
+        return 1;
     }
     size_t n_readings = (size_t)mr->rp.n_readings;
     size_t per_frame = (size_t)s->n_channels * s->n_rows_raw;
@@ -258,38 +274,47 @@ extern "C" int ctbb_phantom_project_host(const struct recon_metadata *mr,
             }
     }
     delete s;
-    return CTBB_OK;
+    return 0;
 }
 
-extern "C" int ctbb_phantom_project_device(const struct recon_metadata *mr,
-                                           const struct ctbb_phantom_object *objects,
-                                           int n_objects, const float *d_tube_angles,
-                                           const double *d_table_positions, size_t frame0,
-                                           size_t n_frames, float i0, uint64_t seed,
-                                           float *d_out)
+#define SYNTH_CUDA_TRY(expr)                                                          \
+    do {                                                                              \
+        cudaError_t e_ = (expr);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return 5;                                                                 \
+        }                                                                             \
+    } while (0)
+
+extern "C" int synth_project_device(const struct recon_metadata *mr, const struct ctbb_phantom_object *objects,
+                                    int n_objects, const float *d_tube_angles, const double *d_table_positions,
+                                    size_t frame0, size_t n_frames, float i0, uint64_t seed, float *d_out,
+                                    void *stream_ptr)
 {
-    clear_error();
+    g_error[0] = 0;
     if (!d_out || !d_tube_angles || !d_table_positions) {
         set_error("phantom: null device pointer");
-        return CTBB_ERR_ARGUMENT;
+        return 1;
     }
     std::vector<char> host(sizeof(PhantomScan));
     PhantomScan *s = reinterpret_cast<PhantomScan *>(host.data());
     int st = make_scan(mr, objects, n_objects, i0, seed, s);
     if (st) return st;
-    cudaStream_t stream = current_stream();
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_ptr);
+    int dev = 0, sms = 0;
+    SYNTH_CUDA_TRY(cudaGetDevice(&dev));
+    SYNTH_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PhantomScan *d_scan = nullptr;
-    CTBB_CUDA_TRY(cudaMallocAsync((void **)&d_scan, sizeof(PhantomScan), stream));
-    CTBB_CUDA_TRY(cudaMemcpyAsync(d_scan, s, sizeof(PhantomScan), cudaMemcpyHostToDevice, stream));
+    SYNTH_CUDA_TRY(cudaMallocAsync((void **)&d_scan, sizeof(PhantomScan), stream));
+    SYNTH_CUDA_TRY(cudaMemcpyAsync(d_scan, s, sizeof(PhantomScan), cudaMemcpyHostToDevice, stream));
     size_t total = (size_t)s->n_channels * s->n_rows_raw * n_frames;
-    int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)num_sms() * 16);
+    int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 16);
     if (blocks < 1) blocks = 1;
     phantom_project_kernel<<<blocks, 256, 0, stream>>>(d_scan, d_tube_angles, d_table_positions,
                                                       (size_t)mr->rp.n_readings, frame0, n_frames,
                                                       d_out);
-    count_launch();
-    CTBB_CUDA_TRY(cudaGetLastError());
-    CTBB_CUDA_TRY(cudaFreeAsync(d_scan, stream));
-    CTBB_CUDA_TRY(cudaStreamSynchronize(stream));
-    return CTBB_OK;
+    SYNTH_CUDA_TRY(cudaGetLastError());
+    SYNTH_CUDA_TRY(cudaFreeAsync(d_scan, stream));
+    SYNTH_CUDA_TRY(cudaStreamSynchronize(stream));
+    return 0;
 }

@@ -357,11 +357,14 @@ int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
    separately although consecutive windows share most of their frames): the
    union of all blocks' pull windows is adaptive-filtered, rebinned and
    ramp-filtered once, and each block is backprojected from its offset into
-   it.  Same plan, block order and output as ctbb_reconstruct_device; the one
-   difference is that the adaptive filter's 18- and 180-degree statistics
-   windows run over the union instead of stopping at each block's window
-   edges, so the images differ where that filter acts near those edges.
-   Device memory: the union window's filtered raw data and rebinned rows. */
+   it.  Same plan, block order and output as ctbb_reconstruct_device.  The
+   reference's adaptive filter stops its 18- and 180-degree statistics at
+   each block's window ends, so the views a block reads from frames near those
+   ends are re-made from the block's own window; the remaining difference to
+   the block loop is the rounding of the rebin's view coordinate, which the
+   union takes in split (integer + fraction) form (0.15 HU max over a
+   40-turn scan of 13 blocks, 1472 x 128 rebinned rows).  Device memory: the union window's filtered raw
+   data and rebinned rows, one block window and its re-made views. */
 int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan,
                                  float *d_final, float mu_water);
 
@@ -402,10 +405,6 @@ int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float 
 int ctbb_profile_enable(int on);
 int ctbb_profile_read(double *ms, uint64_t *launches, int n, int reset);
 
-/* Measured FP32 FMA throughput of the current device (best of `repeats`
-   launches of a register-only FMA loop), TFLOP/s; -1 without a device. */
-double ctbb_fp32_peak_tflops(int repeats);
-
 /* Bytes of device workspace ctbb_reconstruct_device keeps for this plan. */
 size_t ctbb_workspace_bytes(const struct recon_metadata *mr);
 
@@ -418,20 +417,6 @@ int ctbb_release_workspace(void);
 
 /* Number of kernels this library launched since load (all entry points). */
 uint64_t ctbb_kernel_launch_count(void);
-
-/* ------------------------------------------------------------------------- */
-/* Synthetic helical phantom (test and benchmark input; not on the hot path). */
-/* ------------------------------------------------------------------------- */
-
-/* One phantom object: an ellipsoid (kind 1) or an infinite z-cylinder (kind 0)
-   with attenuation mu (added to what lies beneath) [1/mm]. */
-struct ctbb_phantom_object {
-    int kind;
-    float mu;
-    float center[3];
-    float semi_axes[3];
-    float rotation[9];          /* row-major world->body rotation */
-};
 
 /* ---- contexts: concurrent scans ----------------------------------------
    The reference keeps its state in per-translation-unit globals and runs one
@@ -512,23 +497,6 @@ int ctbb_server_wait(ctbb_server srv, uint64_t ticket, struct ctbb_request_resul
    their results, stop the workers, free their contexts.  No call on srv may
    start after this one. */
 int ctbb_server_destroy(ctbb_server srv);
-
-/* Forward-project n_objects into frames [frame0, frame0+n_frames) of a helical
-   FFS scan described by mr->cg / mr->rp and the tables mr->tube_angles,
-   mr->table_positions (length rp.n_readings).  i0 > 0 adds Poisson noise with
-   that unattenuated count (seeded; counter-based so host and device agree
-   up to libm rounding).  out: [n_frames][n_rows_raw][n_channels] line integrals.
-   The host variant runs on the CPU; the device variant takes device pointers
-   for out and the two tables. */
-int ctbb_phantom_project_host(const struct recon_metadata *mr,
-                              const struct ctbb_phantom_object *objects, int n_objects,
-                              size_t frame0, size_t n_frames, float i0, uint64_t seed,
-                              float *out);
-int ctbb_phantom_project_device(const struct recon_metadata *mr,
-                                const struct ctbb_phantom_object *objects, int n_objects,
-                                const float *d_tube_angles, const double *d_table_positions,
-                                size_t frame0, size_t n_frames, float i0, uint64_t seed,
-                                float *d_out);
 
 #ifdef __cplusplus
 } /* extern "C" */

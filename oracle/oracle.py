@@ -20,7 +20,9 @@ from ctbangbang_gb300.structs import ReconMetadata, ReconParams
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libctbb_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libctbb_ref.so")
-REFERENCE_TREE = os.environ.get("CTBB_REFERENCE_TREE", "/root/reference")
+# The reference source tree, named by the environment (no default: the
+# reference build is made only where its sources are present).
+REFERENCE_TREE = os.environ.get("CTBB_REFERENCE_TREE")
 
 _MR = C.POINTER(ReconMetadata)
 _F = C.POINTER(C.c_float)
@@ -38,7 +40,7 @@ def build_oracle():
 def build_reference():
     """Compiles the reference CPU path if its sources are present; returns the
     library path or None."""
-    if not os.path.isdir(os.path.join(REFERENCE_TREE, "src")):
+    if not REFERENCE_TREE or not os.path.isdir(os.path.join(REFERENCE_TREE, "src")):
         return REF_LIB if os.path.exists(REF_LIB) else None
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REFERENCE_TREE], check=True)
     return REF_LIB
@@ -47,8 +49,8 @@ def build_reference():
 def oracle():
     global _oracle
     if _oracle is None:
-        src = os.path.join(HERE, "ctbb_oracle.cpp")
-        if not os.path.exists(ORACLE_LIB) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
+        srcs = [os.path.join(HERE, f) for f in ("ctbb_oracle.cpp", "ctbb_oracle_plan.cpp")]
+        if not os.path.exists(ORACLE_LIB) or any(os.path.getmtime(ORACLE_LIB) < os.path.getmtime(f) for f in srcs):
             build_oracle()
         lib = C.CDLL(ORACLE_LIB)
         protos = {
@@ -66,6 +68,12 @@ def oracle():
             "oracle64_backproject_range": (C.c_int, [_MR, _F, C.c_int, C.c_int, _D]),
             "oracle_rebin_views": (C.c_int, [_MR, _F, C.c_int, C.c_int, _F]),
             "oracle_backproject_patch": (C.c_int, [_MR, _F, C.c_int, C.c_int, C.c_int, C.c_int, _F]),
+            "oracle_configure_recon_params": (C.c_int, [C.c_char_p, C.POINTER(ReconParams)]),
+            "oracle_configure_ct_geom": (C.c_int, [_MR]),
+            "oracle_configure_reconstruction": (C.c_int, [_MR]),
+            "oracle_update_block_info": (C.c_int, [_MR]),
+            "oracle_free_plan": (C.c_int, [_MR]),
+            "oracle_ramp_taps": (C.c_int, [C.c_int, C.c_float, C.c_float, C.c_float, _F]),
             "oracle_interp2": (C.c_float, [_F, C.c_int, C.c_int, C.c_float, C.c_float]),
             "oracle_interp3": (C.c_float, [_F, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]),
         }

@@ -9,6 +9,8 @@ import numpy as np
 from ctbangbang_gb300 import lib as _lib
 from ctbangbang_gb300 import scans
 
+import ctbb_synth
+
 HU_PER_MU = 1000.0 / scans.MU_WATER   # 1 HU = mu_water / 1000
 
 
@@ -39,8 +41,8 @@ class Scan:
         self.workdir = workdir
         self.prm, self.install = scans.prepare(spec, workdir)
         self.mr = scans.plan(self.prm, self.install)
-        self.objects = scans.phantom_objects(spec)
-        self.frames = scans.project_host(self.mr, self.objects, 0, spec.n_readings,
+        self.objects = ctbb_synth.phantom_objects(spec)
+        self.frames = ctbb_synth.project_host(self.mr, self.objects, 0, spec.n_readings,
                                          spec.i0 if noise else 0.0, spec.seed)
         scans.write_raw(os.path.join(workdir, "scan.raw"), self.frames)
 

@@ -178,3 +178,58 @@ def test_fp32_reference_path_vs_fp64_oracle(lib, oracle_lib, tmp_path, z_ffs, ph
     assert np.abs(f64).max() > 0.01
     assert mx <= 0.1 and rms <= 0.01, (mx, rms)
     scan.close()
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "plan_*.json"))),
+                         ids=lambda p: os.path.basename(p))
+def test_oracle_planner_bit_exact_vs_reference_golden(oracle_lib, tmp_path, path):
+    """The oracle's planner restatement (used by the benchmark's reference arm,
+    which must not load the reconstruction library) reproduces the reference
+    planner's integers and float tables exactly, from the .prm and .scanner
+    files it parses itself."""
+    import hashlib
+
+    from ctbangbang_gb300 import structs
+    from oracle import plan as OP
+    fx = json.load(open(path))
+    keep = {k: v for k, v in fx["spec"].items() if k in scans.ScanSpec.__dataclass_fields__}
+    spec = scans.ScanSpec(**keep)
+    mr = OP.plan_spec(spec, str(tmp_path))
+    n = spec.n_readings
+    for k, v in fx["geom"].items():
+        assert np.float32(getattr(mr.cg, k)) == np.float32(v), k
+    assert np.float32(mr.rp.end_pos) == np.float32(fx["rp_end_pos"])
+
+    def ri_of(ri):
+        d = {f: getattr(ri, f) for f, _ in structs.ReconInfo._fields_ if f != "cb"}
+        d.update({"cb." + f: getattr(ri.cb, f) for f, _ in structs.BlockInfo._fields_})
+        return d
+
+    got = ri_of(mr.ri)
+    for k, v in fx["plan"].items():
+        assert (np.float32(got[k]) == np.float32(v)) if isinstance(v, float) else got[k] == v, k
+    assert hashlib.sha256(C.string_at(mr.tube_angles, 4 * n)).hexdigest() == fx["tube_angles_sha256"]
+    assert hashlib.sha256(C.string_at(mr.table_positions, 8 * n)).hexdigest() == fx["table_positions_sha256"]
+    blocks = OP.block_plans(mr)
+    assert len(blocks) == len(fx["blocks"]) == mr.ri.n_blocks
+    for ri, blk in zip(blocks, fx["blocks"]):
+        got = ri_of(ri)
+        for k, v in blk.items():
+            assert (np.float32(got[k]) == np.float32(v)) if isinstance(v, float) else got[k] == v, (k, got[k], v)
+    OP.free_plan(mr)
+
+
+def test_oracle_ramp_taps_match_reference_sharp_kernel(oracle_lib):
+    """resources/ramp.m restated in the oracle equals the reference's shipped
+    f_<N>_sharp taps (the ramp formula with c = a = 1, ds = r_f sin(fai/2))."""
+    kat = json.load(open(os.path.join(GOLDEN, "ramp_kat.json")))
+    geo = {"f_736_sharp": (595.0, 0.067864 * 3.1415926535897 / 180.0),   # Definition AS
+           "f_672_sharp": (570.0, 0.07758621 * 3.1415926535897 / 180.0)}  # Sensation 64
+    for name, fx in kat.items():
+        r_f, fai = geo[name]
+        n_os = fx["n_os"]
+        taps = np.zeros(2 * n_os, np.float32)
+        ds = np.float32(r_f * np.sin(np.float32(fai) / 2.0))
+        oracle_lib.oracle_ramp_taps(n_os, C.c_float(float(ds)), 1.0, 1.0, taps.ctypes.data_as(C.POINTER(C.c_float)))
+        np.testing.assert_allclose(taps[n_os - 8:n_os + 9], fx["centre_taps"], rtol=0, atol=2e-7)
+        assert abs(taps.astype(np.float64).sum() - fx["sum"]) < 1e-5
