@@ -53,7 +53,11 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="config2")
+    ap.add_argument("--config", default="config3",
+                    help="headline workload (config3: the largest single-GPU configuration)")
+    ap.add_argument("--beside", default="config2",
+                    help="a second workload measured after the headline and reported beside it ('' for none)")
+    ap.add_argument("--no-hu", action="store_true", help="skip the HU errors of the output against the oracle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--file", action="store_true",
@@ -208,91 +212,296 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
-# CPU baseline: the oracle port (the reference CPU path's algorithm) on host cores
+# The reference CPU path's arithmetic (the oracle port) on host threads
 # --------------------------------------------------------------------------
 
-def cpu_baseline(spec, mr, blocks, sizes, threads=None, steps=1, warmup=0, sub_frames=1024, angles_per_thread=1):
-    """Bounded sample of the whole step on every host core: each thread runs
-    (a) adaptive filter + FFS rebin + ramp filter of its own 1024-frame
-    sub-window of block 0 and (b) the backprojection of one half-turn angle of
-    block 0 (512^2 x 32 voxels x n_half_turns).  The full-scan CPU time is
-    composed from the per-frame and per-angle rates of those samples; VU/s is
-    that scan's voxel updates over the composed time."""
-    from ctbangbang_gb300 import scans, structs
+def _ranges(n, parts):
+    """[a, b) ranges splitting n items into `parts` nearly equal pieces."""
+    parts = max(1, min(parts, n))
+    edges = [n * i // parts for i in range(parts + 1)]
+    return [(edges[i], edges[i + 1]) for i in range(parts) if edges[i + 1] > edges[i]]
+
+
+def block_meta(mr, ri):
+    """A copy of the plan whose recon_info is the given block's."""
+    from ctbangbang_gb300 import structs
+    m = structs.ReconMetadata()
+    C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
+    m.ri = ri
+    m.ctd.raw = m.ctd.rebin = m.ctd.image = None
+    return m
+
+
+def n_views_of(mb):
+    return mb.ri.n_proj_pull // mb.ri.n_ffs - 2 * mb.cg.add_projections
+
+
+def oracle_rows(orc, mb, raw, taps, threads, views=None, double=False):
+    """Ramp-filtered rebinned rows of one block from its raw window
+    [P][R_raw][N] (float32): the adaptive filter of the whole window on one
+    thread (the reference's own is one call per window), then the rebin of
+    views [v0, v1) and their ramp filter split over `threads`.  float: the
+    reference CPU path's arithmetic; double: the FP64 oracle.  Returns the rows
+    [n_views][n_rows][n_os] (only [v0, v1) written) and the stage times (s)."""
+    nv = n_views_of(mb)
+    v0, v1 = views if views else (0, nv)
+    R, N = mb.cg.n_rows, mb.cg.n_channels_oversampled
+    D = C.POINTER(C.c_double)
+    Fp = C.POINTER(C.c_float)
+    taps_p = taps.ctypes.data_as(Fp)
+    t = {}
+    t0 = time.perf_counter()
+    if double:
+        filt = np.empty(raw.size, np.float64)
+        orc.oracle64_adaptive_filter(C.byref(mb), raw.ctypes.data_as(Fp), filt.ctypes.data_as(D))
+        rows = np.zeros(nv * R * N, np.float64)
+    else:
+        filt = np.ascontiguousarray(raw, np.float32).copy()
+        mb.ctd.raw = filt.ctypes.data_as(Fp)
+        orc.oracle_adaptive_filter(C.byref(mb))
+        mb.ctd.raw = None
+        rows = np.zeros(nv * R * N, np.float32)
+    t["adaptive_filter"] = time.perf_counter() - t0
+    view = R * N
+
+    def rebin_part(r):
+        if double:
+            orc.oracle64_rebin_views(C.byref(mb), filt.ctypes.data_as(D), v0 + r[0], v0 + r[1],
+                                     rows.ctypes.data_as(D))
+        else:
+            orc.oracle_rebin_views(C.byref(mb), filt.ctypes.data_as(Fp), v0 + r[0], v0 + r[1],
+                                   rows.ctypes.data_as(Fp))
+
+    def filter_part(r):
+        off = (v0 * R + r[0]) * N
+        if double:
+            orc.oracle64_filter_rows(rows[off:].ctypes.data_as(D), r[1] - r[0], N, taps_p)
+        else:
+            orc.oracle_filter_rows(rows[off:].ctypes.data_as(Fp), r[1] - r[0], N, taps_p)
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        t0 = time.perf_counter()
+        list(ex.map(rebin_part, _ranges(v1 - v0, 4 * threads)))
+        t["rebin"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        list(ex.map(filter_part, _ranges((v1 - v0) * R, 4 * threads)))
+        t["ramp_filter"] = time.perf_counter() - t0
+    del filt
+    assert view * nv == rows.size
+    return rows, t
+
+
+def oracle_patch(orc, mb, rows, patch, double=False):
+    """Backprojection (all angles) of the pixels x in [x0, x1), y in [y0, y1)
+    of one block from its filtered rows -> [n_slices_block][y1-y0][x1-x0]."""
+    x0, x1, y0, y1 = patch
+    nx, ny, nz = mb.rp.nx, mb.rp.ny, mb.ri.n_slices_block
+    out = np.zeros(nz * ny * nx, np.float64 if double else np.float32)
+    if double:
+        D = C.POINTER(C.c_double)
+        orc.oracle64_backproject_patch(C.byref(mb), rows.ctypes.data_as(D), x0, x1, y0, y1, out.ctypes.data_as(D))
+    else:
+        Fp = C.POINTER(C.c_float)
+        orc.oracle_backproject_patch(C.byref(mb), rows.ctypes.data_as(Fp), x0, x1, y0, y1, out.ctypes.data_as(Fp))
+    return out.reshape(nz, ny, nx)[:, y0:y1, x0:x1].copy()
+
+
+def oracle_taps(orc, mb):
+    taps = np.zeros(2 * mb.cg.n_channels_oversampled, np.float32)
+    if orc.oracle_load_filter(C.byref(mb), taps.ctypes.data_as(C.POINTER(C.c_float))) != 0:
+        raise RuntimeError("oracle: no reconstruction kernel file under %s" % mb.install_dir.decode())
+    return taps
+
+
+# A step of the CPU sample, on block 0 of the workload: the adaptive filter of
+# 1/CPU_AF_PARTS of its pull window (one thread: the reference filters a
+# window in one call), the rebin and ramp filter of 1/CPU_VIEW_PARTS of its
+# views and the backprojection of 1/CPU_ANGLE_PARTS of its half-turn angles
+# (every voxel of the block, all half turns), the last two over all host
+# threads.  The block's time is composed as CPU_AF_PARTS t_af +
+# CPU_VIEW_PARTS t_rebin+filter + CPU_ANGLE_PARTS t_bp, the scan's as the sum
+# over its blocks (equal windows).  Each part is a different slice of the
+# block from step to step.
+CPU_AF_PARTS = 4
+CPU_VIEW_PARTS = 32
+CPU_ANGLE_PARTS = 64
+
+
+def cpu_sample_step(orc, mb, raw, taps, threads, step):
+    """One step of the CPU sample (see above); returns its stage times (s)."""
+    from ctbangbang_gb300 import structs
+    Fp = C.POINTER(C.c_float)
+    t_step = time.perf_counter()
+    t = {}
+    # adaptive filter of a sub-window (whole focal-spot cycles)
+    P, n_ffs = int(mb.ri.n_proj_pull), int(mb.ri.n_ffs)
+    frame = mb.cg.n_rows_raw * mb.cg.n_channels
+    sub = (P // CPU_AF_PARTS) // n_ffs * n_ffs
+    f0 = ((step * sub) % max(P - sub, 1)) // n_ffs * n_ffs
+    ms = structs.ReconMetadata()
+    C.memmove(C.byref(ms), C.byref(mb), C.sizeof(ms))
+    ms.ri.n_proj_pull = sub
+    win = raw[f0 * frame:(f0 + sub) * frame].copy()
+    ms.ctd.raw = win.ctypes.data_as(Fp)
+    t0 = time.perf_counter()
+    orc.oracle_adaptive_filter(C.byref(ms))
+    t["adaptive_filter"] = time.perf_counter() - t0
+    del win
+    # rebin + ramp filter of a view range (from the unfiltered window: the
+    # cost does not depend on the values)
+    nv = n_views_of(mb)
+    R, N = mb.cg.n_rows, mb.cg.n_channels_oversampled
+    part = nv // CPU_VIEW_PARTS
+    v0 = (step * part) % max(nv - part, 1)
+    rows = np.zeros(nv * R * N, np.float32)
+    raw_p = raw.ctypes.data_as(Fp)
+    taps_p = taps.ctypes.data_as(Fp)
+
+    def rebin_part(r):
+        orc.oracle_rebin_views(C.byref(mb), raw_p, v0 + r[0], v0 + r[1], rows.ctypes.data_as(Fp))
+
+    def filter_part(r):
+        orc.oracle_filter_rows(rows[(v0 * R + r[0]) * N:].ctypes.data_as(Fp), r[1] - r[0], N, taps_p)
+
+    n_half = mb.cg.n_proj_turn // 2
+    n_ang = max(n_half // CPU_ANGLE_PARTS, 1)
+    a0 = (step * n_ang) % max(n_half - n_ang, 1)
+    plane_block = mb.rp.nx * mb.rp.ny * mb.ri.n_slices_block
+
+    def bp(r):
+        out = np.zeros(plane_block, np.float32)
+        orc.oracle_backproject_range(C.byref(mb), rows.ctypes.data_as(Fp), a0 + r[0], a0 + r[1],
+                                     out.ctypes.data_as(Fp))
+
+    # the rebin's per-call set-up (the reference splits the window by focal
+    # spot once per block, rebin_filter_cpu.cu:418-645): timed alone with a
+    # call that rebins no view, and counted once per block
+    t0 = time.perf_counter()
+    orc.oracle_rebin_views(C.byref(mb), raw_p, v0, v0, rows.ctypes.data_as(Fp))
+    t["rebin_setup"] = time.perf_counter() - t0
+    with cf.ThreadPoolExecutor(threads) as ex:
+        t0 = time.perf_counter()
+        list(ex.map(rebin_part, _ranges(part, threads)))
+        t["rebin"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        list(ex.map(filter_part, _ranges(part * R, 4 * threads)))
+        t["ramp_filter"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        list(ex.map(bp, _ranges(n_ang, threads)))
+        t["backproject"] = time.perf_counter() - t0
+    t["step"] = time.perf_counter() - t_step
+    rebin_views = max(t["rebin"] - t["rebin_setup"], 0.0)
+    t["block_s"] = (CPU_AF_PARTS * t["adaptive_filter"] + t["rebin_setup"] +
+                    CPU_VIEW_PARTS * (rebin_views + t["ramp_filter"]) + CPU_ANGLE_PARTS * t["backproject"])
+    return t
+
+
+def cpu_sample_text(threads, mb, n_blocks):
+    nht = n_views_of(mb) // (mb.cg.n_proj_turn // 2)
+    return ("%d threads; a step: the adaptive filter of 1/%d of block 0's pull window (%d frames; one thread), "
+            "the rebin and ramp filter of 1/%d of its %d views and the backprojection of 1/%d of its %d half-turn "
+            "angles (%d x %d x %d voxels x %d half turns), the last two over all threads; scan time composed as "
+            "%d x (%d t_af + t_rebin_setup + %d (t_rebin - t_rebin_setup + t_filter) + %d t_backproject), "
+            "t_rebin_setup the rebin's per-call split of the window by focal spot, timed alone; finalize "
+            "omitted (< 0.1%% of the CPU time)"
+            % (threads, CPU_AF_PARTS, mb.ri.n_proj_pull, CPU_VIEW_PARTS, n_views_of(mb), CPU_ANGLE_PARTS,
+               mb.cg.n_proj_turn // 2, mb.rp.nx, mb.rp.ny, mb.ri.n_slices_block, nht, n_blocks, CPU_AF_PARTS,
+               CPU_VIEW_PARTS, CPU_ANGLE_PARTS))
+
+
+def window_from_device(d_scan, ri, n_readings, frame):
+    """A block's pull window from the resident scan (frames outside the scan are zeros)."""
+    s = int(ri.idx_pull_start)
+    s = s - 2 ** 64 if s >= 2 ** 63 else s
+    P = int(ri.n_proj_pull)
+    out = np.zeros(P * frame, np.float32)
+    a, e = max(s, 0), min(s + P, n_readings)
+    if e > a:
+        out[(a - s) * frame:(e - s) * frame] = d_scan[a * frame:e * frame].cpu().numpy()
+    return out
+
+
+def cpu_baseline(mr, blocks, sizes, raw0, steps=1, threads=None):
+    """The CPU sample (cpu_sample_step) on block 0's window raw0."""
     from oracle import oracle as O
     orc = O.oracle()
     T = threads or os.cpu_count() or 1
+    mb = block_meta(mr, blocks[0])
+    taps = oracle_taps(orc, mb)
+    res = [cpu_sample_step(orc, mb, raw0, taps, T, k) for k in range(steps)]
+    block_s = statistics.median(r["block_s"] for r in res)
+    scan_s = len(blocks) * block_s
+    return dict(value=sizes["vu_total"] / scan_s, unit="voxel-updates/s", cores=T, kind="port",
+                sample=cpu_sample_text(T, mb, len(blocks)), scan_seconds=scan_s,
+                step_seconds=statistics.median(r["step"] for r in res))
+
+
+# --------------------------------------------------------------------------
+# HU errors of the benched output on sampled patches
+# --------------------------------------------------------------------------
+
+def hu_check(mr, blocks, d_scan, d_final, n_readings, threads=None):
+    """HU errors of the GPU's final stack against the FP64 oracle and against
+    the reference CPU path's float arithmetic (the oracle port), on two 32 x 32
+    patches (image centre and off-centre) of the middle block: the oracle
+    filters, rebins and ramp-filters that block's own pull window and
+    backprojects the patches; the final slices whose finalize weights all fall
+    on that block are compared at the patch pixels."""
+    from ctbangbang_gb300 import scans
+    from oracle import oracle as O
+    orc = O.oracle()
+    T = threads or os.cpu_count() or 1
+    b = len(blocks) // 2
+    mb = block_meta(mr, blocks[b])
     frame = mr.cg.n_rows_raw * mr.cg.n_channels
-    b0 = blocks[0]
-    # host raw of T distinct sub-windows (generated on the CPU)
-    subs = []
-    objs = ctbb_synth.phantom_objects(spec)
-    s0 = int(b0.idx_pull_start)
+    nx, ny, nb = mr.rp.nx, mr.rp.ny, mr.ri.n_slices_block
+    raw = window_from_device(d_scan, blocks[b], n_readings, frame)
+    taps = oracle_taps(orc, mb)
+    t0 = time.perf_counter()
+    rows32, _ = oracle_rows(orc, mb, raw, taps, T)
+    rows64, _ = oracle_rows(orc, mb, raw, taps, T, double=True)
+    h, w = 32, 32
+    patches = [(nx // 2 - w // 2, nx // 2 + w // 2, ny // 2 - h // 2, ny // 2 + h // 2),
+               (nx // 4 - w // 2, nx // 4 + w // 2, (5 * ny) // 8 - h // 2, (5 * ny) // 8 + h // 2)]
+    jobs = [(p, dbl) for p in patches for dbl in (False, True)]
+    with cf.ThreadPoolExecutor(len(jobs)) as ex:
+        imgs = list(ex.map(lambda j: oracle_patch(orc, mb, rows64 if j[1] else rows32, j[0], j[1]), jobs))
+    del rows32, rows64
+    n_final = orc.oracle_n_slices_final(C.byref(mr))
+    n_raw = nb * mr.ri.n_blocks
+    wts = np.zeros(n_raw, np.float64)
+    src = np.zeros(n_raw, np.int32)
+    plane = nx * ny
+    gpu = d_final.reshape(n_final, ny, nx)
+    d64, d32, ref_err = [], [], []
+    slices = []
+    for k in range(n_final):
+        orc.oracle64_finalize_weights(C.byref(mr), k, wts.ctypes.data_as(C.POINTER(C.c_double)),
+                                      src.ctypes.data_as(C.POINTER(C.c_int)))
+        used = np.nonzero(wts)[0]
+        if not len(used) or not all(b * nb <= src[s] < (b + 1) * nb for s in used):
+            continue
+        slices.append(k)
+        for pi, p in enumerate(patches):
+            x0, x1, y0, y1 = p
+            e32 = sum(wts[s] * imgs[2 * pi][src[s] - b * nb].astype(np.float64) for s in used)
+            e64 = sum(wts[s] * imgs[2 * pi + 1][src[s] - b * nb] for s in used)
+            g = gpu[k, y0:y1, x0:x1].double().cpu().numpy()
+            d64.append((g - e64).ravel())
+            d32.append((g - e32).ravel())
+            ref_err.append((e32 - e64).ravel())
+    hu = 1000.0 / scans.MU_WATER
 
-    def gen(t):
-        start = s0 + (t * sub_frames) % max(b0.n_proj_pull - sub_frames, 1)
-        start -= start % mr.ri.n_ffs
-        return ctbb_synth.project_host(mr, objs, start, sub_frames, spec.i0, spec.seed)
+    def stats(parts):
+        v = np.concatenate(parts) * hu
+        return {"max": float(np.abs(v).max()), "rms": float(np.sqrt(np.mean(v ** 2)))}
 
-    with cf.ThreadPoolExecutor(T) as ex:
-        subs = list(ex.map(gen, range(T)))
-
-    def sub_meta(raw):
-        m = structs.ReconMetadata()
-        C.memmove(C.byref(m), C.byref(mr), C.sizeof(m))
-        m.ri = b0
-        m.ri.n_proj_pull = sub_frames
-        nv = sub_frames // m.ri.n_ffs - 2 * m.cg.add_projections
-        rb = np.zeros(nv * m.cg.n_rows * m.cg.n_channels_oversampled, np.float32)
-        r = raw.reshape(-1).copy()
-        m.ctd.raw = r.ctypes.data_as(C.POINTER(C.c_float))
-        m.ctd.rebin = rb.ctypes.data_as(C.POINTER(C.c_float))
-        return m, r, rb
-
-    # block-0 filtered rows for the backprojection sample (values do not
-    # change the CPU cost; real pages are touched)
-    mb = structs.ReconMetadata()
-    C.memmove(C.byref(mb), C.byref(mr), C.sizeof(mb))
-    mb.ri = b0
-    rebin_full = np.full(sizes["rebin_samples"][0], 0.01, np.float32)
-    n_half = mr.cg.n_proj_turn // 2
-
-    def run_a(t):
-        m, r, rb = sub_meta(subs[t])
-        orc.oracle_adaptive_filter(C.byref(m))
-        orc.oracle_rebin_filter(C.byref(m))
-        return 0
-
-    def run_b(t):
-        out = np.zeros(mr.rp.nx * mr.rp.ny * mr.ri.n_slices_block, np.float32)
-        i0 = (t * 37) % n_half
-        orc.oracle_backproject_range(C.byref(mb), rebin_full.ctypes.data_as(C.POINTER(C.c_float)), i0,
-                                     i0 + angles_per_thread, out.ctypes.data_as(C.POINTER(C.c_float)))
-        return 0
-
-    results = []
-    for it in range(warmup + steps):
-        with cf.ThreadPoolExecutor(T) as ex:
-            t0 = time.perf_counter()
-            list(ex.map(run_a, range(T)))
-            ta = time.perf_counter() - t0
-            t0 = time.perf_counter()
-            list(ex.map(run_b, range(T)))
-            tb = time.perf_counter() - t0
-        if it >= warmup:
-            per_frame = ta / (T * sub_frames)                  # s per raw frame (a), all cores busy
-            per_angle = tb / (T * angles_per_thread)          # s per half-turn angle (b)
-            scan_s = sum(ri.n_proj_pull for ri in blocks) * per_frame + len(blocks) * n_half * per_angle
-            results.append(dict(value=sizes["vu_total"] / scan_s, scan_s=scan_s, ta=ta, tb=tb))
-    best = statistics.median(r["value"] for r in results)
-    sample = ("%d threads; per step each thread: adaptive filter + phi/z-FFS rebin + ramp filter of a "
-              "%d-frame sub-window of block 0, then the backprojection of %d half-turn angle(s) of block 0 "
-              "(512^2 x 32 voxels x %d half turns); full-scan time composed from those per-frame and "
-              "per-angle rates over the %d frames and %d angles of the 3-block scan (finalize omitted, "
-              "< 0.1%% of the CPU time)" % (T, sub_frames, angles_per_thread, sizes["nht"][0],
-                                           sum(ri.n_proj_pull for ri in blocks), len(blocks) * n_half))
-    return dict(value=best, unit="voxel-updates/s", cores=T, kind="port", sample=sample,
-                scan_seconds=statistics.median(r["scan_s"] for r in results))
+    return {"hu_vs_fp64": stats(d64), "hu_vs_reference": stats(d32), "reference_vs_fp64": stats(ref_err),
+            "block": b, "final_slices": len(slices), "patches": patches, "pixels": int(sum(x.size for x in d64)),
+            "oracle_s": time.perf_counter() - t0,
+            "how": "block %d's own pull window through the oracle (float: the reference CPU path's arithmetic; "
+                   "double: FP64), two 32 x 32 patches backprojected, compared with the GPU stack at the %d final "
+                   "slices whose finalize weights all fall on that block" % (b, len(slices))}
 
 
 # --------------------------------------------------------------------------
@@ -300,33 +509,73 @@ def cpu_baseline(spec, mr, blocks, sizes, threads=None, steps=1, warmup=0, sub_f
 # --------------------------------------------------------------------------
 
 def run_reference(args):
+    """The reference CPU path (the oracle port: a bit-exact restatement of
+    rebin_filter_cpu / backproject_cpu and of the adaptive filter's kernels)
+    on the machine's host cores, on our arm's workload.  It plans with the
+    oracle's restatement of the reference planner and projects its input with
+    the test library's CPU projector: the reconstruction library is never
+    loaded.  Each step is the bounded CPU sample of cpu_sample_step; the
+    full-scan time is composed from the step's stage times."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from ctbangbang_gb300 import scans
+    from oracle import oracle as O
+    from oracle import plan as OP
+    orc = O.oracle()
     spec = scans.CONFIGS[args.config]
-    with tempfile.TemporaryDirectory(prefix="ctbb_bench_") as d:
-        mr = make_plan(spec, d)
-        blocks = block_plans(mr)
+    T = os.cpu_count() or 1
+    t_wall = time.perf_counter()
+    with tempfile.TemporaryDirectory(prefix="ctbb_bench_ref_") as d:
+        mr = OP.plan_spec(spec, d)
+        blocks = OP.block_plans(mr)
         sizes = workload_sizes(mr, blocks)
-        warm = max(args.warmup, 3) if args.warmup else 0
+        n_final = orc.oracle_n_slices_final(C.byref(mr))
+        mb = block_meta(mr, blocks[0])
+        frame = mr.cg.n_rows_raw * mr.cg.n_channels
+        s0, P = int(blocks[0].idx_pull_start), int(blocks[0].n_proj_pull)
+        objs = ctbb_synth.phantom_objects(spec)
+        raw = np.zeros((P, frame), np.float32)
+
+        def gen(r):
+            a, e = max(s0 + r[0], 0), min(s0 + r[1], spec.n_readings)
+            if e > a:
+                raw[a - s0:e - s0] = ctbb_synth.project_host(mr, objs, a, e - a, spec.i0, spec.seed).reshape(e - a, -1)
+
         t0 = time.perf_counter()
-        cb = cpu_baseline(spec, mr, blocks, sizes, steps=args.steps, warmup=min(warm, 1))
-        wall = time.perf_counter() - t0
-        scans.free_plan(mr)
-    v = cb["value"]
+        with cf.ThreadPoolExecutor(T) as ex:
+            list(ex.map(gen, _ranges(P, 8 * T)))
+        gen_s = time.perf_counter() - t0
+        raw = raw.reshape(-1)
+        taps = oracle_taps(orc, mb)
+        for k in range(args.warmup):
+            cpu_sample_step(orc, mb, raw, taps, T, k)
+        res = []
+        t_timed = time.perf_counter()
+        for k in range(args.steps):
+            res.append(cpu_sample_step(orc, mb, raw, taps, T, args.warmup + k))
+        timed_s = time.perf_counter() - t_timed
+        workload = workload_text(args.config, spec, mr, len(blocks), n_final)
+        OP.free_plan(mr)
+    step_ms = timed_s * 1e3 / args.steps
+    block_s = statistics.median(r["block_s"] for r in res)
+    scan_s = len(blocks) * block_s
+    v = sizes["vu_total"] / scan_s
     line = {
         "impl": "reference", "metric": "voxel-updates/s", "value": v, "unit": "voxel-updates/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": cb["scan_seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded helical phantom (config-2 geometry)",
-        "config": {"workload": workload_text(args.config, spec, mr, len(blocks), None),
-                   "voxel_updates_per_scan": sizes["vu_total"], "scans_per_s": 1.0 / cb["scan_seconds"],
-                   "wall_s": wall,
-                   "note": "reference CPU path as restated bit-exactly by the oracle port (the reference's "
-                           "own sources build only where the reference tree is present)"},
-        "cpu_baseline": {"value": v, "unit": "voxel-updates/s", "cores": cb["cores"], "kind": "port",
-                         "sample": cb["sample"]},
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic seeded helical phantom (water cylinder + ellipsoids, Poisson noise), projected on the CPU",
+        "config": {"workload": workload, "voxel_updates_per_scan": sizes["vu_total"],
+                   "composed_scan_seconds": scan_s, "scans_per_s": 1.0 / scan_s,
+                   "step_stage_seconds": {k: statistics.median(r[k] for r in res)
+                                          for k in ("adaptive_filter", "rebin_setup", "rebin", "ramp_filter",
+                                                    "backproject")},
+                   "input_generation_s": gen_s, "wall_s": time.perf_counter() - t_wall,
+                   "note": "value = the scan's voxel updates over its composed CPU time; ms_per_step = the "
+                           "measured time of one sample step (real work, not extrapolated)"},
+        "cpu_baseline": {"value": v, "unit": "voxel-updates/s", "cores": T, "kind": "port",
+                         "sample": cpu_sample_text(T, mb, len(blocks))},
         "e2e": {"value": v, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -356,23 +605,37 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def run_ours(args):
-    import torch
+def time_h2d_d2h(torch, h_scan, n_bytes_h2d, n_bytes_d2h, reps=3):
+    """Pinned host->device and device->host copy times (ms) of the given
+    sizes alone, on a stream of their own (the e2e breakdown)."""
+    st = torch.cuda.Stream()
+    dst = torch.empty(n_bytes_h2d // 4, dtype=torch.float32, device="cuda")
+    back = torch.empty(max(n_bytes_d2h // 4, 1), dtype=torch.float32, pin_memory=True)
+    src_d = torch.empty_like(back, device="cuda")
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    h2d, d2h = [], []
+    with torch.cuda.stream(st):
+        for _ in range(reps):
+            e[0].record(st)
+            dst.copy_(h_scan[:dst.numel()], non_blocking=True)
+            e[1].record(st)
+            back.copy_(src_d, non_blocking=True)
+            e[2].record(st)
+            st.synchronize()
+            h2d.append(e[0].elapsed_time(e[1]))
+            d2h.append(e[1].elapsed_time(e[2]))
+    del dst, src_d, back
+    return min(h2d), min(d2h)
 
+
+def measure_config(args, torch, lib, config, rank, world, dist, headline):
+    """One workload: the device-resident step (value), the host-buffer step
+    (e2e) with its breakdown, and -- for the headline -- the other path, the
+    per-stage profile, the clocks and the HU errors of the output."""
     from ctbangbang_gb300 import lib as L
     from ctbangbang_gb300 import scans
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    lib = L.load()
-    lib.ctbb_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream))
-    spec = scans.CONFIGS[args.config]
+    spec = scans.CONFIGS[config]
     tmp = tempfile.TemporaryDirectory(prefix="ctbb_bench_")
     mr = make_plan(spec, tmp.name)
     blocks = block_plans(mr)
@@ -381,29 +644,30 @@ def run_ours(args):
     frame = mr.cg.n_rows_raw * mr.cg.n_channels
     plane = mr.rp.nx * mr.rp.ny
     n_final = lib.ctbb_n_slices_final(C.byref(mr))
+    out = {"workload": workload_text(config, spec, mr, len(blocks), n_final), "sizes": sizes, "spec": spec,
+           "mr": mr, "blocks": blocks, "tmp": tmp, "n_final": n_final}
 
     # synthetic scan on the device (each replica its own seed)
     d_scan = ctbb_synth.project_scan_device(torch, mr, spec, seed=replica_seed(spec.seed, rank))
     d_final = torch.empty(n_final * plane, dtype=torch.float32, device="cuda")
-
     entry = {"scan": ("ctbb_reconstruct_scan_device", "ctbb_reconstruct_scan_host"),
              "blocks": ("ctbb_reconstruct_device", "ctbb_reconstruct_host")}
     other_path = "blocks" if args.path == "scan" else "scan"
     dev_entry, host_entry = entry[args.path]
     alt_dev, alt_host = entry[other_path]
     h2d_key = {"scan": "union_h2d_bytes", "blocks": "h2d_bytes"}
+    out.update(dev_entry=dev_entry, host_entry=host_entry, h2d_bytes=sizes[h2d_key[args.path]])
 
     def step():
-        L.call(dev_entry, C.byref(mr), C.c_void_p(d_scan.data_ptr()),
-               C.c_void_p(d_final.data_ptr()), C.c_float(0.0))
+        L.call(dev_entry, C.byref(mr), C.c_void_p(d_scan.data_ptr()), C.c_void_p(d_final.data_ptr()),
+               C.c_float(0.0))
 
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-
-    clocks = ClockSampler(local) if rank == 0 else None
+    clocks = ClockSampler(local) if (rank == 0 and headline) else None
     lib.ctbb_profile_read(None, None, 0, 1)
-    lib.ctbb_profile_enable(1)
+    lib.ctbb_profile_enable(1 if headline else 0)
     launches0 = lib.ctbb_kernel_launch_count()
     if dist is not None:
         dist.barrier()
@@ -416,22 +680,20 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-    launches = lib.ctbb_kernel_launch_count() - launches0
+    out["launches"] = lib.ctbb_kernel_launch_count() - launches0
     lib.ctbb_profile_enable(0)
     stage_ms = (C.c_double * 5)()
     stage_n = (C.c_uint64 * 5)()
     lib.ctbb_profile_read(stage_ms, stage_n, 5, 1)
-    clk = clocks.stop() if clocks else None
+    out["stage_ms"], out["stage_n"] = list(stage_ms), list(stage_n)
+    out["clocks"] = clocks.stop() if clocks else None
     per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    ms = total_ms / args.steps
-    ms = max_over_ranks(ms, dist)
-    value = world * sizes["vu_total"] / (ms * 1e-3)
+    ms = max_over_ranks(ev[0].elapsed_time(ev[-1]) / args.steps, dist)
+    out.update(ms=ms, per_step=per_step, value=world * sizes["vu_total"] / (ms * 1e-3))
 
     # e2e through the host-buffer entry point (pinned host scan and stack)
-    e2e = None
+    out["e2e"] = None
     ws_e2e = None
-    e2e_file = None
     if not args.no_e2e:
         h_scan = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
         h_scan.copy_(d_scan)
@@ -448,37 +710,42 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        c0 = time.thread_time()
         for _ in range(args.steps):
             e2e_step()
         torch.cuda.synchronize()
-        e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-        e_ms = max_over_ranks(e_ms, dist)
+        e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
+        cpu_ms = (time.thread_time() - c0) * 1e3 / args.steps
         same = bool(torch.equal(h_final.cuda(), d_final))
-        e2e = {"value": world * sizes["vu_total"] / (e_ms * 1e-3), "unit": "voxel-updates/s",
-               "h2d_bytes_per_step": sizes[h2d_key[args.path]], "d2h_bytes_per_step": n_final * plane * 4,
-               "ms_per_step": e_ms, "matches_device_path": same, "entry_point": host_entry}
-        if not args.no_whole_scan:
-            # the other path from the same pinned buffers
+        h2d_ms, d2h_ms = time_h2d_d2h(torch, h_scan, out["h2d_bytes"], n_final * plane * 4)
+        out["e2e"] = {
+            "value": world * sizes["vu_total"] / (e_ms * 1e-3), "unit": "voxel-updates/s",
+            "h2d_bytes_per_step": out["h2d_bytes"], "d2h_bytes_per_step": n_final * plane * 4,
+            "ms_per_step": e_ms, "matches_device_path": same, "entry_point": host_entry,
+            "breakdown_ms": {
+                "device_step": ms, "e2e_minus_device": e_ms - ms,
+                "h2d_copy_alone": h2d_ms, "d2h_copy_alone": d2h_ms,
+                "h2d_gbs": out["h2d_bytes"] / (h2d_ms * 1e-3) / 1e9,
+                "calling_thread_cpu": cpu_ms,
+                "note": "the host path streams the copy in chunks under the compute: e2e = device step + the "
+                        "first chunk's copy + what does not overlap; calling_thread_cpu includes the wait "
+                        "for the stream (a spinning synchronise)"}}
+        if headline and not args.no_whole_scan:
             def ws_host_step():
                 L.call(alt_host, C.byref(mr), hp, fp, C.c_float(0.0))
 
             for _ in range(2):
                 ws_host_step()
-            if dist is not None:
-                dist.barrier()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             for _ in range(args.steps):
                 ws_host_step()
             torch.cuda.synchronize()
-            ws_e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-            ws_e_ms = max_over_ranks(ws_e_ms, dist)
+            ws_e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
             ws_e2e = {"value": world * sizes["vu_total"] / (ws_e_ms * 1e-3), "unit": "voxel-updates/s",
                       "h2d_bytes_per_step": sizes[h2d_key[other_path]], "d2h_bytes_per_step": n_final * plane * 4,
                       "ms_per_step": ws_e_ms, "entry_point": alt_host}
-        if args.file:
-            # the whole-scan path reading the plan's raw file (written once,
-            # outside the timed region; the file cache holds it afterwards)
+        if headline and args.file:
             raw_path = os.path.join(mr.rp.raw_data_dir.decode(), mr.rp.raw_data_file.decode())
             h_scan.numpy().tofile(raw_path)
 
@@ -493,23 +760,20 @@ def run_ours(args):
                 file_step()
             torch.cuda.synchronize()
             f_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
-            e2e_file = {"value": world * sizes["vu_total"] / (f_ms * 1e-3), "unit": "voxel-updates/s",
-                        "read_bytes_per_step": sizes["union_h2d_bytes"], "ms_per_step": f_ms,
-                        "matches_device_path": bool(torch.equal(h_final.cuda(), d_final))
-                        if args.path == "scan" else None,
-                        "entry_point": "ctbb_reconstruct_scan_file"}
+            out["e2e_file"] = {"value": world * sizes["vu_total"] / (f_ms * 1e-3), "unit": "voxel-updates/s",
+                               "read_bytes_per_step": sizes["union_h2d_bytes"], "ms_per_step": f_ms,
+                               "entry_point": "ctbb_reconstruct_scan_file"}
             os.remove(raw_path)
         del h_scan, h_final
 
-    # the other path (block loop or whole scan) on the same resident scan, and
-    # how far its stack is from this path's
-    whole = None
-    if not args.no_whole_scan:
+    # the other path (block loop or whole scan) on the same resident scan
+    out["other_path"] = None
+    if headline and not args.no_whole_scan:
         d_final2 = torch.empty_like(d_final)
 
         def ws_step():
-            L.call(alt_dev, C.byref(mr), C.c_void_p(d_scan.data_ptr()),
-                   C.c_void_p(d_final2.data_ptr()), C.c_float(0.0))
+            L.call(alt_dev, C.byref(mr), C.c_void_p(d_scan.data_ptr()), C.c_void_p(d_final2.data_ptr()),
+                   C.c_float(0.0))
 
         for _ in range(max(args.warmup, 3)):
             ws_step()
@@ -524,18 +788,58 @@ def run_ours(args):
         ws_ms = w0.elapsed_time(w1) / args.steps
         diff = (d_final2 - d_final).double().abs()
         hu = 1000.0 / scans.MU_WATER
-        whole = {"path": other_path, "value": world * sizes["vu_total"] / (ws_ms * 1e-3),
-                 "unit": "voxel-updates/s", "ms_per_step": ws_ms,
-                 "max_hu_between_paths": float(diff.max()) * hu,
-                 "rms_hu_between_paths": float(diff.pow(2).mean().sqrt()) * hu,
-                 "entry_point": alt_dev, "e2e": ws_e2e}
+        out["other_path"] = {"path": other_path, "value": world * sizes["vu_total"] / (ws_ms * 1e-3),
+                             "unit": "voxel-updates/s", "ms_per_step": ws_ms,
+                             "max_hu_between_paths": float(diff.max()) * hu,
+                             "rms_hu_between_paths": float(diff.pow(2).mean().sqrt()) * hu,
+                             "entry_point": alt_dev, "e2e": ws_e2e}
+        del d_final2
+    out["d_scan"], out["d_final"] = d_scan, d_final
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = L.load()
+    lib.ctbb_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    m = measure_config(args, torch, lib, args.config, rank, world, dist, headline=True)
+    mr, blocks, sizes = m["mr"], m["blocks"], m["sizes"]
+    plane = mr.rp.nx * mr.rp.ny
+    spec = m["spec"]
 
     if rank != 0:
+        del m
         if dist is not None:
             dist.destroy_process_group()
         return
 
+    # HU errors of the benched output (sampled patches of the middle block)
+    hu = None
+    if not args.no_hu:
+        try:
+            hu = hu_check(mr, blocks, m["d_scan"], m["d_final"], spec.n_readings)
+        except Exception as e:  # reported in the line, the rest of the run stands
+            hu = {"error": "%s: %s" % (type(e).__name__, e)}
+    raw0 = None
+    if world == 1 and not args.no_cpu_baseline:
+        raw0 = window_from_device(m["d_scan"], blocks[0], spec.n_readings, mr.cg.n_rows_raw * mr.cg.n_channels)
+    del m["d_scan"], m["d_final"]
+    torch.cuda.empty_cache()
+
     # roofline of the dominant kernel (backprojection, FP32-pipe bound)
+    stage_ms, stage_n = m["stage_ms"], m["stage_n"]
     peak_fp32 = ctbb_synth.fp32_peak_tflops(5, torch.cuda.current_stream().cuda_stream)
     bp_ms, bp_n = stage_ms[3], max(stage_n[3], 1)
     vu_per_launch = sizes["vu_total"] / len(blocks)
@@ -544,59 +848,78 @@ def run_ours(args):
     traffic = read_traffic().get("backproject")
     peaks, peak_kind = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # HBM-bound stages: algorithmic bytes per stage pass over its measured
-    # time; a pass covers the union window on the whole-scan path and one
-    # block's window on the block loop
     if args.path == "scan":
         raw_b, rb_b = sizes["union_raw_samples"], sizes["union_rebin_samples"]
     else:
         nblk = len(blocks)
         raw_b = sum(sizes["raw_samples"]) / nblk
         rb_b = sum(sizes["rebin_samples"]) / nblk
+    n_final = m["n_final"]
     stage_bytes = {"adaptive_filter": 8 * raw_b, "rebin": 4 * raw_b + 4 * rb_b, "ramp_filter": 8 * rb_b,
                    "finalize": 4 * plane * (mr.ri.n_slices_recon + n_final)}
     stages = {}
     for i, name in enumerate(STAGES):
         if stage_n[i] == 0:
             continue
-        t_launch = stage_ms[i] / stage_n[i]
         entry = {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_n[i] / args.steps,
                  "share": stage_ms[i] / max(sum(stage_ms), 1e-9)}
         if name in stage_bytes:
-            gbs = stage_bytes[name] / (t_launch * 1e-3) / 1e9
-            entry.update({"achieved_gbs": gbs, "frac_of_hbm": gbs / hbm})
+            # algorithmic bytes of one pass over the union (or one block window)
+            passes = 1 if args.path == "scan" else len(blocks)
+            gbs = stage_bytes[name] * passes / (stage_ms[i] / args.steps * 1e-3) / 1e9
+            entry.update({"achieved_gbs_per_pass": gbs, "frac_of_hbm": gbs / hbm})
         stages[name] = entry
+
+    # the other configuration, reported beside the headline
+    beside = None
+    if world == 1 and args.beside and args.beside != args.config:
+        try:
+            mb = measure_config(args, torch, lib, args.beside, rank, world, dist, headline=False)
+            beside = {"workload": mb["workload"], "value": mb["value"], "unit": "voxel-updates/s",
+                      "ms_per_step": mb["ms"], "scans_per_s": 1e3 / mb["ms"],
+                      "voxel_updates_per_scan": mb["sizes"]["vu_total"], "e2e": mb["e2e"],
+                      "entry_point": mb["dev_entry"]}
+            del mb["d_scan"], mb["d_final"]
+            scans.free_plan(mb["mr"])
+        except Exception as e:
+            beside = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
+
     serve = None
     if world == 1 and not args.no_serve:
-        del d_scan
-        torch.cuda.empty_cache()
         try:
             serve = serve_measure(args, torch)
         except Exception as e:  # reported in the line, the rest of the run stands
             serve = {"error": "%s: %s" % (type(e).__name__, e)}
     cpu = None
-    if world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(spec, mr, blocks, sizes, steps=1, warmup=0)
-    per_step_sorted = sorted(per_step)
+    if raw0 is not None:
+        cpu = cpu_baseline(mr, blocks, sizes, raw0, steps=1)
+    per_step_sorted = sorted(m["per_step"])
+    ms = m["ms"]
     line = {
-        "metric": "voxel-updates/s", "value": value, "unit": "voxel-updates/s", "n_gpus": world,
+        "metric": "voxel-updates/s", "value": m["value"], "unit": "voxel-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic seeded helical phantom (config-2 geometry), generated on the device",
+        "data": "synthetic seeded helical phantom (water cylinder + ellipsoids, Poisson noise), generated on the device",
         "config": {
-            "workload": workload_text(args.config, spec, mr, len(blocks), n_final),
+            "workload": m["workload"],
             "path": ("whole scan: the union of the blocks' pull windows (%d frames) adaptive-filtered, rebinned "
-                     "and ramp-filtered once, each block backprojected from it (%s / %s)"
-                     % (sizes["union_h2d_bytes"] // (4 * frame), dev_entry, host_entry)) if args.path == "scan" else
+                     "and ramp-filtered once, each block's edge views re-made from its own window, each block "
+                     "backprojected (%s / %s)" % (sizes["union_h2d_bytes"] // (4 * mr.cg.n_rows_raw *
+                                                                                  mr.cg.n_channels),
+                                                  m["dev_entry"], m["host_entry"]))
+                    if args.path == "scan" else
                     ("block loop as the reference: each block's pull window filtered, rebinned and backprojected "
-                     "(%s / %s)" % (dev_entry, host_entry)),
+                     "(%s / %s)" % (m["dev_entry"], m["host_entry"])),
             "scans_per_s": world / (ms * 1e-3),
             "voxel_updates_per_scan": sizes["vu_total"],
-            "latency_ms": {"p50": per_step_sorted[len(per_step) // 2],
-                           "p99": per_step_sorted[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]},
-            "l2": "no flush: each step reads %.1f GB of raw frames (> 129 MB L2)" % (sizes[h2d_key[args.path]] / 1e9),
+            "latency_ms": {"p50": per_step_sorted[len(per_step_sorted) // 2],
+                           "p99": per_step_sorted[min(len(per_step_sorted) - 1,
+                                                      int(math.ceil(0.99 * len(per_step_sorted))) - 1)]},
+            "l2": "no flush: each step reads %.1f GB of raw frames (> 129 MB L2)" % (m["h2d_bytes"] / 1e9),
             "parallelism": "replicas" if world > 1 else "single GPU",
         },
+        "hu": hu,
         "roofline": {"kernel": "backproject_kernel", "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                      "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 > 0 else None,
                      "traffic": traffic, "flop_per_vu": FLOP_PER_VU, "vu_per_launch": vu_per_launch,
@@ -606,12 +929,13 @@ def run_ours(args):
         "stages": stages,
         "hbm_peak_gbs": hbm, "hbm_peak_kind": peak_kind,
         "cpu_baseline": cpu,
-        "e2e": e2e,
-        "other_path": whole,
-        "e2e_file": e2e_file,
+        "e2e": m["e2e"],
+        "other_path": m["other_path"],
+        "e2e_file": m.get("e2e_file"),
+        "beside": beside,
         "serve": serve,
-        "gpu_launches": launches / args.steps,
-        "clocks": clk,
+        "gpu_launches": m["launches"] / args.steps,
+        "clocks": m["clocks"],
     }
     print(json.dumps(line), flush=True)
     scans.free_plan(mr)

@@ -8,6 +8,7 @@
 #include <unistd.h>
 
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -225,8 +226,29 @@ int require_device(Context &c)
     return CTBB_OK;
 }
 
-// the library-wide context's device (the no-allocation path, the peak probe)
-int require_device() { return require_device(ctx()); }
+// A usable CUDA device, without binding the library-wide context to it (the
+// no-allocation filter holds no buffers of that context).
+int require_device()
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error("no CUDA device available (%s); this library has no CPU path",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        return CTBB_ERR_NO_DEVICE;
+    }
+    return CTBB_OK;
+}
+
+// The adaptive filter on the library-wide stream with the caller's scratch,
+// serialised with the other entry points and counted by the stage profile.
+int run_adaptive_filter_with(const struct recon_metadata &mr, const float *d_in, float *d_out, float *d_scratch)
+{
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    StageScope scope(c, 0);
+    return launch_adaptive_filter(mr, d_in, d_out, d_scratch, c.stream);
+}
 
 // ---- stage implementations (device pointers, stream-ordered) --------------
 
@@ -313,7 +335,9 @@ extern "C" const char *ctbb_version(void) { return "ctbangbang_gb300 0.1.0 (sm_1
 
 extern "C" int ctbb_set_stream(void *stream)
 {
-    ctx().stream = reinterpret_cast<cudaStream_t>(stream);
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.stream = reinterpret_cast<cudaStream_t>(stream);
     return CTBB_OK;
 }
 
@@ -466,19 +490,26 @@ extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
     return 2 * raw + rebin + image;
 }
 
-// Waits for the context's copy and compute streams when a reconstruction
-// returns, so that once a call has returned -- also one that failed halfway,
-// say on a missing filter file after its first copies were enqueued -- no
-// copy from the caller's host buffer and no kernel writing the caller's
-// output is still in flight.  After a successful call both are idle already.
-struct StreamsDrained {
-    Context &c;
-    ~StreamsDrained()
-    {
-        if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
-        cudaStreamSynchronize(c.stream);
+// Runs a reconstruction body and then waits for the context's copy and
+// compute streams, so that once a call has returned -- also one that failed
+// halfway, say on a missing filter file after its first copies were enqueued
+// -- no copy from the caller's host buffer and no kernel writing the caller's
+// output is still in flight.  After a successful body both are idle already;
+// a device fault that only surfaces in this wait is the call's error (a
+// failing body keeps its own first error).
+template <class Body>
+static int drained(Context &c, Body &&body)
+{
+    int st = body();
+    cudaError_t e1 = c.copy_stream ? cudaStreamSynchronize(c.copy_stream) : cudaSuccess;
+    cudaError_t e2 = cudaStreamSynchronize(c.stream);
+    if (st == CTBB_OK && (e1 != cudaSuccess || e2 != cudaSuccess)) {
+        set_error("device work of this call failed: %s",
+                  cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        return CTBB_ERR_CUDA;
     }
-};
+    return st;
+}
 
 static int reconstruct_device_in(Context &c, struct recon_metadata *mr, const float *d_scan, float *d_final,
                                        float mu_water)
@@ -491,46 +522,47 @@ static int reconstruct_device_in(Context &c, struct recon_metadata *mr, const fl
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
-    StreamsDrained drained{c};
-    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
-    const size_t n_readings = (size_t)mr->rp.n_readings;
-    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
-    const size_t n_block = mr->ri.n_slices_block;
-    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
-    mr->ri.cb.block_idx = 0;
-    for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
-        struct recon_info ri;
-        CTBB_TRY(plan_next_block(*mr, &ri));
-        mr->ri = ri;
-        BlockDims d = block_dims(*mr);
-        // the block's pull window: a view into the resident scan when it lies
-        // inside the data, else a zero-filled copy (frames past either end read 0)
-        long long s0 = (long long)(int)mr->ri.idx_pull_start;
-        long long s1 = s0 + (long long)d.n_proj_pull;
-        const float *d_win = nullptr;
-        if (s0 >= 0 && s1 <= (long long)n_readings) {
-            d_win = d_scan + (size_t)s0 * frame;
-        } else {
-            CTBB_TRY(c.raw_in.ensure(d.raw_elems() * sizeof(float)));
-            CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, d.raw_elems() * sizeof(float), c.stream));
-            long long a = s0 < 0 ? 0 : s0, e = s1 > (long long)n_readings ? (long long)n_readings : s1;
-            if (e > a)
-                CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - s0) * frame,
-                                              d_scan + (size_t)a * frame, (size_t)(e - a) * frame * sizeof(float),
-                                              cudaMemcpyDeviceToDevice, c.stream));
-            d_win = c.raw_in.as<float>();
+    return drained(c, [&]() -> int {
+        const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+        const size_t n_readings = (size_t)mr->rp.n_readings;
+        const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+        const size_t n_block = mr->ri.n_slices_block;
+        CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+        mr->ri.cb.block_idx = 0;
+        for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
+            struct recon_info ri;
+            CTBB_TRY(plan_next_block(*mr, &ri));
+            mr->ri = ri;
+            BlockDims d = block_dims(*mr);
+            // the block's pull window: a view into the resident scan when it lies
+            // inside the data, else a zero-filled copy (frames past either end read 0)
+            long long s0 = (long long)(int)mr->ri.idx_pull_start;
+            long long s1 = s0 + (long long)d.n_proj_pull;
+            const float *d_win = nullptr;
+            if (s0 >= 0 && s1 <= (long long)n_readings) {
+                d_win = d_scan + (size_t)s0 * frame;
+            } else {
+                CTBB_TRY(c.raw_in.ensure(d.raw_elems() * sizeof(float)));
+                CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, d.raw_elems() * sizeof(float), c.stream));
+                long long a = s0 < 0 ? 0 : s0, e = s1 > (long long)n_readings ? (long long)n_readings : s1;
+                if (e > a)
+                    CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - s0) * frame,
+                                                  d_scan + (size_t)a * frame, (size_t)(e - a) * frame * sizeof(float),
+                                                  cudaMemcpyDeviceToDevice, c.stream));
+                d_win = c.raw_in.as<float>();
+            }
+            CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
+            CTBB_TRY(do_adaptive(c, *mr, d_win, c.raw_filt.as<float>()));
+            CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
+            CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+            CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
+            float *slab = c.image.as<float>() + b * n_block * plane;
+            CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab));
         }
-        CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
-        CTBB_TRY(do_adaptive(c, *mr, d_win, c.raw_filt.as<float>()));
-        CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
-        CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
-        CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
-        float *slab = c.image.as<float>() + b * n_block * plane;
-        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab));
-    }
-    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
-    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return CTBB_OK;
+        CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
+        CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        return CTBB_OK;
+    });
 }
 
 extern "C" int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
@@ -710,71 +742,72 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
-    StreamsDrained drained{c};
-    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
-    const long long n_readings = (long long)mr->rp.n_readings;
-    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
-    const size_t n_block = mr->ri.n_slices_block;
-    std::vector<struct recon_info> blocks;
-    long long g0 = 0, g1 = 0;
-    struct recon_metadata mg;
-    CTBB_TRY(plan_union(mr, &blocks, &g0, &g1, &mg));
-    BlockDims dg = block_dims(mg);
-    const float *d_win = nullptr;
-    if (g0 >= 0 && g1 <= n_readings) {
-        d_win = d_scan + (size_t)g0 * frame;
-    } else {
-        CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
-        CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, dg.raw_elems() * sizeof(float), c.stream));
-        long long a = g0 < 0 ? 0 : g0, e = g1 > n_readings ? n_readings : g1;
-        if (e > a)
-            CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - g0) * frame, d_scan + (size_t)a * frame,
-                                          (size_t)(e - a) * frame * sizeof(float), cudaMemcpyDeviceToDevice,
-                                          c.stream));
-        d_win = c.raw_in.as<float>();
-    }
-    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
-    CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    size_t max_pull = 0, max_patch = 0;
-    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
-    const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
-    CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
-    {
-        StageScope scope(c, 0);
-        CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
-    }
-    const size_t view_elems = dg.n_rows * dg.n_os;
-    CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * view_elems) * sizeof(float)));
-    RebinTables rt;
-    CTBB_TRY(build_rebin_tables(mg, &rt));
-    rt.split_view_coord = 1;  // the union's frame offsets are large
-    CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
-    {
-        StageScope scope(c, 1);
-        CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
-    }
-    CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
-    if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
-    for (size_t b = 0; b < blocks.size(); ++b) {
-        mr->ri = blocks[b];
-        // view j of block b is view j + (pull_start_b - g0) / n_ffs of the
-        // union, except its edge views, re-made after the union's rows
-        ViewRows vr;
-        vr.off = union_view_offset(blocks[b], g0);
-        EdgePlan e = edge_plan(*mr, g0, g1);
-        vr.d0 = e.d0;
-        vr.d1 = e.d1;
-        vr.n_used = e.n_used;
-        vr.patch = dg.n_views;
-        if (e.any())
-            CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
-                                    c.rebin.as<float>() + dg.n_views * view_elems));
-        float *slab = c.image.as<float>() + b * n_block * plane;
-        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr));
-    }
-    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
-    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return CTBB_OK;
+    return drained(c, [&]() -> int {
+        const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+        const long long n_readings = (long long)mr->rp.n_readings;
+        const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+        const size_t n_block = mr->ri.n_slices_block;
+        std::vector<struct recon_info> blocks;
+        long long g0 = 0, g1 = 0;
+        struct recon_metadata mg;
+        CTBB_TRY(plan_union(mr, &blocks, &g0, &g1, &mg));
+        BlockDims dg = block_dims(mg);
+        const float *d_win = nullptr;
+        if (g0 >= 0 && g1 <= n_readings) {
+            d_win = d_scan + (size_t)g0 * frame;
+        } else {
+            CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
+            CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, dg.raw_elems() * sizeof(float), c.stream));
+            long long a = g0 < 0 ? 0 : g0, e = g1 > n_readings ? n_readings : g1;
+            if (e > a)
+                CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - g0) * frame, d_scan + (size_t)a * frame,
+                                              (size_t)(e - a) * frame * sizeof(float), cudaMemcpyDeviceToDevice,
+                                              c.stream));
+            d_win = c.raw_in.as<float>();
+        }
+        CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+        CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
+        size_t max_pull = 0, max_patch = 0;
+        edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
+        const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
+        CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
+        {
+            StageScope scope(c, 0);
+            CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
+        }
+        const size_t view_elems = dg.n_rows * dg.n_os;
+        CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * view_elems) * sizeof(float)));
+        RebinTables rt;
+        CTBB_TRY(build_rebin_tables(mg, &rt));
+        rt.split_view_coord = 1;  // the union's frame offsets are large
+        CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
+        {
+            StageScope scope(c, 1);
+            CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
+        }
+        CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
+        if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
+        for (size_t b = 0; b < blocks.size(); ++b) {
+            mr->ri = blocks[b];
+            // view j of block b is view j + (pull_start_b - g0) / n_ffs of the
+            // union, except its edge views, re-made after the union's rows
+            ViewRows vr;
+            vr.off = union_view_offset(blocks[b], g0);
+            EdgePlan e = edge_plan(*mr, g0, g1);
+            vr.d0 = e.d0;
+            vr.d1 = e.d1;
+            vr.n_used = e.n_used;
+            vr.patch = dg.n_views;
+            if (e.any())
+                CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
+                                        c.rebin.as<float>() + dg.n_views * view_elems));
+            float *slab = c.image.as<float>() + b * n_block * plane;
+            CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr));
+        }
+        CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
+        CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        return CTBB_OK;
+    });
 }
 
 extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
@@ -877,6 +910,15 @@ static int finalize_common(struct recon_metadata *mr, float mu_water)
     if (!mr->ctd.image) {
         set_error("finalize_image_stack: ctd.image is null");
         return CTBB_ERR_STATE;
+    }
+    if (mr->table_positions && mr->rp.n_readings > 1000) {
+        // the slice order follows the table's direction (src/finalize_image_stack_cpu.cu:35)
+        double dtp = mr->table_positions[1000] - mr->table_positions[0];
+        if (!std::isfinite(dtp) || dtp == 0.0) {
+            set_error("finalize_image_stack: table positions 0 and 1000 are equal or not finite (the table "
+                      "does not move), so the slice order is undefined");
+            return CTBB_ERR_CONFIG;
+        }
     }
     CTBB_TRY(require_device(ctx()));
     Context &c = ctx();
@@ -1126,9 +1168,10 @@ static int reconstruct_scan_host_in(Context &c, struct recon_metadata *mr, const
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
-    StreamsDrained drained{c};
-    HostFeed feed(h_scan, (long long)mr->rp.n_readings, mr->cg.n_rows_raw * mr->cg.n_channels);
-    return scan_streamed(c, mr, feed, h_final, mu_water);
+    return drained(c, [&]() -> int {
+        HostFeed feed(h_scan, (long long)mr->rp.n_readings, mr->cg.n_rows_raw * mr->cg.n_channels);
+        return scan_streamed(c, mr, feed, h_final, mu_water);
+    });
 }
 
 extern "C" int ctbb_reconstruct_scan_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
@@ -1290,11 +1333,12 @@ static int reconstruct_scan_file_in(Context &c, struct recon_metadata *mr, float
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
-    StreamsDrained drained{c};
-    char path[4096 + 255 + 2];
-    snprintf(path, sizeof(path), "%s/%s", mr->rp.raw_data_dir, mr->rp.raw_data_file);
-    FileFeed feed(path, (long long)mr->rp.raw_data_offset, mr->cg.n_rows_raw * mr->cg.n_channels);
-    return scan_streamed(c, mr, feed, h_final, mu_water);
+    return drained(c, [&]() -> int {
+        char path[4096 + 255 + 2];
+        snprintf(path, sizeof(path), "%s/%s", mr->rp.raw_data_dir, mr->rp.raw_data_file);
+        FileFeed feed(path, (long long)mr->rp.raw_data_offset, mr->cg.n_rows_raw * mr->cg.n_channels);
+        return scan_streamed(c, mr, feed, h_final, mu_water);
+    });
 }
 
 extern "C" int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float mu_water)
@@ -1313,55 +1357,56 @@ static int reconstruct_host_in(Context &c, struct recon_metadata *mr, const floa
     CTBB_TRY(check_mr(mr));
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
-    StreamsDrained drained{c};
-    CTBB_TRY(ensure_copy_stream(c));
-    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
-    const long long n_readings = mr->rp.n_readings;
-    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
-    const size_t n_block = mr->ri.n_slices_block;
-    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
-    int n_final = ctbb_n_slices_final(mr);
-    CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
-    DeviceBuffer *win[2] = {&c.raw_in, &c.raw_in2};
-    mr->ri.cb.block_idx = 0;
-    for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
-        struct recon_info ri;
-        CTBB_TRY(plan_next_block(*mr, &ri));
-        mr->ri = ri;
-        BlockDims d = block_dims(*mr);
-        int slot = (int)(b & 1);
-        CTBB_TRY(win[slot]->ensure(d.raw_elems() * sizeof(float)));
-        // H2D of the block's window on the copy stream, once the buffer's
-        // previous reader (the adaptive filter two blocks back) is done
-        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[slot], 0));
-        long long s0 = (long long)(int)mr->ri.idx_pull_start, s1 = s0 + (long long)d.n_proj_pull;
-        long long a = s0 < 0 ? 0 : s0, e = s1 > n_readings ? n_readings : s1;
-        float *dst = win[slot]->as<float>();
-        if (a > s0) CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(a - s0) * frame * sizeof(float), c.copy_stream));
-        if (e < s1) {
-            long long z0 = e > s0 ? e : s0;
-            CTBB_CUDA_TRY(cudaMemsetAsync(dst + (size_t)(z0 - s0) * frame, 0, (size_t)(s1 - z0) * frame * sizeof(float),
-                                          c.copy_stream));
+    return drained(c, [&]() -> int {
+        CTBB_TRY(ensure_copy_stream(c));
+        const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+        const long long n_readings = mr->rp.n_readings;
+        const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+        const size_t n_block = mr->ri.n_slices_block;
+        CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+        int n_final = ctbb_n_slices_final(mr);
+        CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
+        DeviceBuffer *win[2] = {&c.raw_in, &c.raw_in2};
+        mr->ri.cb.block_idx = 0;
+        for (size_t b = 0; b < mr->ri.n_blocks; ++b) {
+            struct recon_info ri;
+            CTBB_TRY(plan_next_block(*mr, &ri));
+            mr->ri = ri;
+            BlockDims d = block_dims(*mr);
+            int slot = (int)(b & 1);
+            CTBB_TRY(win[slot]->ensure(d.raw_elems() * sizeof(float)));
+            // H2D of the block's window on the copy stream, once the buffer's
+            // previous reader (the adaptive filter two blocks back) is done
+            CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[slot], 0));
+            long long s0 = (long long)(int)mr->ri.idx_pull_start, s1 = s0 + (long long)d.n_proj_pull;
+            long long a = s0 < 0 ? 0 : s0, e = s1 > n_readings ? n_readings : s1;
+            float *dst = win[slot]->as<float>();
+            if (a > s0) CTBB_CUDA_TRY(cudaMemsetAsync(dst, 0, (size_t)(a - s0) * frame * sizeof(float), c.copy_stream));
+            if (e < s1) {
+                long long z0 = e > s0 ? e : s0;
+                CTBB_CUDA_TRY(cudaMemsetAsync(dst + (size_t)(z0 - s0) * frame, 0, (size_t)(s1 - z0) * frame * sizeof(float),
+                                              c.copy_stream));
+            }
+            if (e > a)
+                CTBB_CUDA_TRY(cudaMemcpyAsync(dst + (size_t)(a - s0) * frame, h_scan + (size_t)a * frame,
+                                              (size_t)(e - a) * frame * sizeof(float), cudaMemcpyHostToDevice,
+                                              c.copy_stream));
+            CTBB_CUDA_TRY(cudaEventRecord(c.copied[slot], c.copy_stream));
+            CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copied[slot], 0));
+            CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
+            CTBB_TRY(do_adaptive(c, *mr, dst, c.raw_filt.as<float>()));
+            CTBB_CUDA_TRY(cudaEventRecord(c.consumed[slot], c.stream));
+            CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
+            CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
+            CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
+            CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), c.image.as<float>() + b * n_block * plane));
         }
-        if (e > a)
-            CTBB_CUDA_TRY(cudaMemcpyAsync(dst + (size_t)(a - s0) * frame, h_scan + (size_t)a * frame,
-                                          (size_t)(e - a) * frame * sizeof(float), cudaMemcpyHostToDevice,
-                                          c.copy_stream));
-        CTBB_CUDA_TRY(cudaEventRecord(c.copied[slot], c.copy_stream));
-        CTBB_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copied[slot], 0));
-        CTBB_TRY(c.raw_filt.ensure(d.raw_elems() * sizeof(float)));
-        CTBB_TRY(do_adaptive(c, *mr, dst, c.raw_filt.as<float>()));
-        CTBB_CUDA_TRY(cudaEventRecord(c.consumed[slot], c.stream));
-        CTBB_TRY(c.rebin.ensure(d.rebin_elems() * sizeof(float)));
-        CTBB_TRY(do_rebin(c, *mr, c.raw_filt.as<float>(), c.rebin.as<float>()));
-        CTBB_TRY(do_filter(c, *mr, c.rebin.as<float>()));
-        CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), c.image.as<float>() + b * n_block * plane));
-    }
-    CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
-    CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
-                                  cudaMemcpyDeviceToHost, c.stream));
-    CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return CTBB_OK;
+        CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
+        CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
+                                      cudaMemcpyDeviceToHost, c.stream));
+        CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        return CTBB_OK;
+    });
 }
 
 extern "C" int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,

@@ -541,5 +541,5 @@ extern "C" int ctbb_adaptive_filter_device_noalloc(const struct recon_metadata *
     CTBB_TRY(noalloc_scratch(&scratch));
     // Every statistic is written for all frames before it is read, so the
     // previous call's contents need no clearing.
-    return launch_adaptive_filter(*mr, d_in, d_out, scratch, current_stream());
+    return run_adaptive_filter_with(*mr, d_in, d_out, scratch);
 }

@@ -15,8 +15,13 @@ namespace ctbb {
 cudaStream_t current_stream();
 int num_sms();
 void count_launch(uint64_t n = 1);
-// Returns CTBB_OK if a CUDA device is usable, else sets the error text.
+// Returns CTBB_OK if a CUDA device is usable, else sets the error text.  Binds
+// nothing: the library-wide context binds its device at its first compute call.
 int require_device();
+// The adaptive filter of one window on the library-wide stream with the
+// caller's scratch (6 * n_proj_pull floats), under the library-wide lock and
+// counted in the stage profile.
+int run_adaptive_filter_with(const struct recon_metadata &mr, const float *d_in, float *d_out, float *d_scratch);
 
 }  // namespace ctbb
 

@@ -49,6 +49,13 @@ int build_finalize_tables(const struct recon_metadata &mr, FinalizeTables *t)
     }
     int recon_direction = recon_direction_of(rp);
     double dtp = mr.table_positions[1000] - mr.table_positions[0];
+    // the reference divides dtp by |dtp| (src/finalize_image_stack_cpu.cu:35);
+    // a table that does not move (axial scan) has no direction to flip by
+    if (!std::isfinite(dtp) || dtp == 0.0) {
+        set_error("finalize: table positions 0 and 1000 are equal or not finite (the table does not move), "
+                  "so the slice order is undefined");
+        return CTBB_ERR_CONFIG;
+    }
     int table_direction = (int)(dtp / std::fabs(dtp));
     int n_raw = (int)(ri.n_slices_block * ri.n_blocks);
     int n_block = (int)ri.n_slices_block;

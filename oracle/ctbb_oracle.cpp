@@ -701,6 +701,79 @@ int oracle_backproject_patch(const struct recon_metadata *mr, const float *rebin
     return 0;
 }
 
+/* The FP64 oracle's stages one at a time, for callers that split the work
+   over threads: adaptive filter of a float raw window into double; rebin of
+   views [v0, v1) of a double raw window; ramp filter of n double rows;
+   backprojection of the pixels x in [x0, x1), y in [y0, y1) (all angles)
+   from double filtered rows into out_block (written there, zeroed first). */
+int oracle64_adaptive_filter(const struct recon_metadata *mr, const float *raw, double *out)
+{
+    size_t n = mr->ri.n_proj_pull * mr->cg.n_rows_raw * mr->cg.n_channels;
+    std::vector<double> r(raw, raw + n);
+    adaptive_filter<double>(*mr, r.data(), out);
+    return 0;
+}
+
+int oracle64_rebin_views(const struct recon_metadata *mr, const double *raw, int v0, int v1, double *out)
+{
+    rebin<double>(*mr, raw, out, v0, v1);
+    return 0;
+}
+
+int oracle64_filter_rows(double *rows, size_t n_rows, int n, const float *taps)
+{
+    filter_rows<double>(rows, n_rows, n, taps);
+    return 0;
+}
+
+int oracle64_backproject_patch(const struct recon_metadata *mr, const double *rows, int x0, int x1, int y0, int y1,
+                               double *out_block)
+{
+    const size_t nx = mr->rp.nx, ny = mr->rp.ny;
+    for (size_t z = 0; z < mr->ri.n_slices_block; ++z)
+        for (int y = y0; y < y1; ++y)
+            for (int x = x0; x < x1; ++x) out_block[(z * ny + (size_t)y) * nx + (size_t)x] = 0.0;
+    backproject<double>(*mr, rows, 0, (int)(mr->cg.n_proj_turn / 2), out_block, x0, x1, y0, y1);
+    return 0;
+}
+
+/* The FP64 finalize of one final slice k as weights: w_out[s] is the weight
+   (w_s / sum, 0 where finalize skips the raw slice) of raw slice s, and
+   src_out[s] the image slice raw slice s is read from after the block
+   reorder -- final[k][px] = sum_s w_out[s] image[src_out[s]][px], the sum
+   finalize<double> forms.  Returns the number of raw slices. */
+int oracle64_finalize_weights(const struct recon_metadata *mr, int k, double *w_out, int *src_out)
+{
+    const struct recon_params &rp = mr->rp;
+    const struct recon_info &ri = mr->ri;
+    const int nb = (int)ri.n_slices_block;
+    int recon_direction = 1;
+    {
+        float d = rp.end_pos - rp.start_pos;
+        if (d != 0.0f) {
+            recon_direction = (int)(std::fabs(d) / d);
+            if (recon_direction != 1 && recon_direction != -1) recon_direction = 1;
+        }
+    }
+    double dtp = mr->table_positions[1000] - mr->table_positions[0];
+    int table_direction = (int)(dtp / std::fabs(dtp));
+    const int n_raw = (int)(ri.n_slices_block * ri.n_blocks);
+    double loc = (double)rp.start_pos + (double)(recon_direction * k) * (double)rp.slice_thickness;
+    double sum = 0.0;
+    for (int s = 0; s < n_raw; s++) {
+        double raw_loc = (double)ri.recon_start_pos + (double)(recon_direction * s) * (double)rp.coll_slicewidth;
+        w_out[s] = std::max(0.0, 1.0 - std::fabs(raw_loc - loc) / (double)rp.slice_thickness);
+        sum += w_out[s];
+        src_out[s] = (recon_direction != table_direction) ? (s / nb) * nb + (nb - 1 - s % nb) : s;
+    }
+    for (int s = 0; s < n_raw; s++) w_out[s] = w_out[s] != 0.0 ? w_out[s] / sum : 0.0;
+    return n_raw;
+}
+
+/* Final slices of the plan: floor(|end - start| / slice_thickness) + 1
+   (src/finalize_image_stack_cpu.cu:67). */
+int oracle_n_slices_final(const struct recon_metadata *mr) { return n_final_of(*mr); }
+
 int oracle64_finalize(const struct recon_metadata *mr, const double *image, double *final_out)
 {
     finalize<double>(*mr, image, final_out);

@@ -68,6 +68,12 @@ def oracle():
             "oracle64_backproject_range": (C.c_int, [_MR, _F, C.c_int, C.c_int, _D]),
             "oracle_rebin_views": (C.c_int, [_MR, _F, C.c_int, C.c_int, _F]),
             "oracle_backproject_patch": (C.c_int, [_MR, _F, C.c_int, C.c_int, C.c_int, C.c_int, _F]),
+            "oracle64_adaptive_filter": (C.c_int, [_MR, _F, _D]),
+            "oracle64_rebin_views": (C.c_int, [_MR, _D, C.c_int, C.c_int, _D]),
+            "oracle64_filter_rows": (C.c_int, [_D, C.c_size_t, C.c_int, _F]),
+            "oracle64_backproject_patch": (C.c_int, [_MR, _D, C.c_int, C.c_int, C.c_int, C.c_int, _D]),
+            "oracle_n_slices_final": (C.c_int, [_MR]),
+            "oracle64_finalize_weights": (C.c_int, [_MR, C.c_int, _D, C.POINTER(C.c_int)]),
             "oracle_configure_recon_params": (C.c_int, [C.c_char_p, C.POINTER(ReconParams)]),
             "oracle_configure_ct_geom": (C.c_int, [_MR]),
             "oracle_configure_reconstruction": (C.c_int, [_MR]),

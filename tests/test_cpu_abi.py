@@ -244,3 +244,18 @@ def test_load_filter_generates_missing_ramp(lib, tmp_path):
         L.call("ctbb_load_filter", C.byref(mr), t)
     assert e.value.status_name == "CTBB_ERR_IO"
     scans.free_plan(mr)
+
+
+def test_finalize_with_a_table_that_does_not_move_is_a_config_error(lib, tmp_path):
+    """The reference takes the table's direction as dtp / |dtp| with dtp the
+    distance between table positions 0 and 1000 (finalize_image_stack_cpu.cu:35),
+    undefined for an axial scan; the library returns CTBB_ERR_CONFIG instead
+    of ordering the slices by garbage, before it looks for a device."""
+    spec = scans.tiny(0, 0)
+    mr = scans.plan_spec(spec, str(tmp_path))
+    tp = np.ctypeslib.as_array(mr.table_positions, (spec.n_readings,))
+    tp[:] = tp[0]
+    st = lib.ctbb_finalize_image_stack(C.byref(mr))
+    assert L.STATUS[st] == "CTBB_ERR_CONFIG", lib.ctbb_last_error()
+    assert b"does not move" in lib.ctbb_last_error()
+    scans.free_plan(mr)

@@ -84,14 +84,23 @@ def test_served_stream_scans_plan_and_fit(lib):
 
 def test_reference_arm_line_keeps_the_contract():
     """The reference arm (the reference CPU path as the bit-exact port, on the
-    host cores) prints one JSON line with the contract's keys."""
+    host cores) prints one JSON line with the contract's keys, and never maps
+    the reconstruction library: it plans with the oracle and projects its
+    input with the test library's CPU projector.  Run on the small no-FFS
+    workload to stay quick."""
     import json
     env = dict(os.environ)
     for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
         env.pop(k, None)
-    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0"], env=env, capture_output=True, text=True, timeout=900)
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--config', 'config1', "
+            "'--steps', '1', '--warmup', '0']; runpy.run_path(%r, run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', 'libctbb_gb300.so' in maps, 'libctbb_oracle.so' in maps)"
+            % os.path.join(REPO, "bench.py"))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900,
+                       cwd=REPO)
     assert r.returncode == 0, r.stderr[-2000:]
+    assert "MAPPED False True" in r.stdout, r.stdout[-500:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
@@ -100,7 +109,8 @@ def test_reference_arm_line_keeps_the_contract():
         assert k in d, k
     assert d["impl"] == "reference" and d["metric"] == d["unit"] == "voxel-updates/s"
     assert d["value"] > 0 and d["higher_is_better"] is True and d["vs_baseline"] is None
-    assert "config2" in d["config"]["workload"]
+    assert d["config"]["workload"].startswith("config1: 672 ch x 16 rows no FFS")
+    assert d["config"]["composed_scan_seconds"] > 0 and d["ms_per_step"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
