@@ -58,6 +58,8 @@ def parse_args():
     ap.add_argument("--beside", default="config2",
                     help="a second workload measured after the headline and reported beside it ('' for none)")
     ap.add_argument("--no-hu", action="store_true", help="skip the HU errors of the output against the oracle")
+    ap.add_argument("--no-fp16", action="store_true",
+                    help="skip the reduced-storage measurement (tensor-core ramp filter, FP16 footprint rows)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--file", action="store_true",
@@ -440,14 +442,13 @@ def cpu_baseline(mr, blocks, sizes, raw0, steps=1, threads=None):
 # HU errors of the benched output on sampled patches
 # --------------------------------------------------------------------------
 
-def hu_check(mr, blocks, d_scan, d_final, n_readings, threads=None):
-    """HU errors of the GPU's final stack against the FP64 oracle and against
-    the reference CPU path's float arithmetic (the oracle port), on two 32 x 32
-    patches (image centre and off-centre) of the middle block: the oracle
-    filters, rebins and ramp-filters that block's own pull window and
-    backprojects the patches; the final slices whose finalize weights all fall
-    on that block are compared at the patch pixels."""
-    from ctbangbang_gb300 import scans
+def hu_reference(mr, blocks, d_scan, n_readings, threads=None):
+    """The oracle's values at sampled patches of the middle block, for
+    hu_compare: the oracle filters, rebins and ramp-filters that block's own
+    pull window (float: the reference CPU path's arithmetic; double: the FP64
+    oracle) and backprojects two 32 x 32 patches (image centre and
+    off-centre); the final slices whose finalize weights all fall on that
+    block are formed from them in double."""
     from oracle import oracle as O
     orc = O.oracle()
     T = threads or os.cpu_count() or 1
@@ -471,10 +472,7 @@ def hu_check(mr, blocks, d_scan, d_final, n_readings, threads=None):
     n_raw = nb * mr.ri.n_blocks
     wts = np.zeros(n_raw, np.float64)
     src = np.zeros(n_raw, np.int32)
-    plane = nx * ny
-    gpu = d_final.reshape(n_final, ny, nx)
-    d64, d32, ref_err = [], [], []
-    slices = []
+    slices, e32, e64 = [], [], []
     for k in range(n_final):
         orc.oracle64_finalize_weights(C.byref(mr), k, wts.ctypes.data_as(C.POINTER(C.c_double)),
                                       src.ctypes.data_as(C.POINTER(C.c_int)))
@@ -482,26 +480,39 @@ def hu_check(mr, blocks, d_scan, d_final, n_readings, threads=None):
         if not len(used) or not all(b * nb <= src[s] < (b + 1) * nb for s in used):
             continue
         slices.append(k)
-        for pi, p in enumerate(patches):
-            x0, x1, y0, y1 = p
-            e32 = sum(wts[s] * imgs[2 * pi][src[s] - b * nb].astype(np.float64) for s in used)
-            e64 = sum(wts[s] * imgs[2 * pi + 1][src[s] - b * nb] for s in used)
+        for pi in range(len(patches)):
+            e32.append(sum(wts[s] * imgs[2 * pi][src[s] - b * nb].astype(np.float64) for s in used))
+            e64.append(sum(wts[s] * imgs[2 * pi + 1][src[s] - b * nb] for s in used))
+    return {"block": b, "patches": patches, "slices": slices, "e32": e32, "e64": e64, "n_final": n_final,
+            "shape": (ny, nx), "oracle_s": time.perf_counter() - t0}
+
+
+def hu_compare(ref, d_final):
+    """HU errors of a GPU final stack against hu_reference's values."""
+    from ctbangbang_gb300 import scans
+    ny, nx = ref["shape"]
+    gpu = d_final.reshape(ref["n_final"], ny, nx)
+    d64, d32, rr = [], [], []
+    i = 0
+    for k in ref["slices"]:
+        for (x0, x1, y0, y1) in ref["patches"]:
             g = gpu[k, y0:y1, x0:x1].double().cpu().numpy()
-            d64.append((g - e64).ravel())
-            d32.append((g - e32).ravel())
-            ref_err.append((e32 - e64).ravel())
+            d64.append((g - ref["e64"][i]).ravel())
+            d32.append((g - ref["e32"][i]).ravel())
+            rr.append((ref["e32"][i] - ref["e64"][i]).ravel())
+            i += 1
     hu = 1000.0 / scans.MU_WATER
 
     def stats(parts):
         v = np.concatenate(parts) * hu
         return {"max": float(np.abs(v).max()), "rms": float(np.sqrt(np.mean(v ** 2)))}
 
-    return {"hu_vs_fp64": stats(d64), "hu_vs_reference": stats(d32), "reference_vs_fp64": stats(ref_err),
-            "block": b, "final_slices": len(slices), "patches": patches, "pixels": int(sum(x.size for x in d64)),
-            "oracle_s": time.perf_counter() - t0,
+    return {"hu_vs_fp64": stats(d64), "hu_vs_reference": stats(d32), "reference_vs_fp64": stats(rr),
+            "block": ref["block"], "final_slices": len(ref["slices"]), "patches": ref["patches"],
+            "pixels": int(sum(x.size for x in d64)), "oracle_s": ref["oracle_s"],
             "how": "block %d's own pull window through the oracle (float: the reference CPU path's arithmetic; "
                    "double: FP64), two 32 x 32 patches backprojected, compared with the GPU stack at the %d final "
-                   "slices whose finalize weights all fall on that block" % (b, len(slices))}
+                   "slices whose finalize weights all fall on that block" % (ref["block"], len(ref["slices"]))}
 
 
 # --------------------------------------------------------------------------
@@ -798,6 +809,66 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
     return out
 
 
+def measure_fp16(args, torch, lib, m, ref):
+    """The reduced-storage mode on the headline scan: the ramp filter as the
+    BF16 hi/lo Toeplitz contraction on the tensor cores writing FP16 footprint
+    rows with per-view scales, the backprojector reading them (FP32
+    accumulation).  Device-resident steps, stage profile, tensor-pipe
+    throughput of the filter, HU errors of the output against the FP64 oracle
+    and against the float32 path's output."""
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+    mr, sizes = m["mr"], m["sizes"]
+    d_scan, d_ref = m["d_scan"], m["d_final"]
+    d_out = torch.empty_like(d_ref)
+    L.call("ctbb_set_storage", L.STORAGE_FP16)
+    try:
+        def step():
+            L.call(m["dev_entry"], C.byref(mr), C.c_void_p(d_scan.data_ptr()), C.c_void_p(d_out.data_ptr()),
+                   C.c_float(0.0))
+
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        lib.ctbb_profile_read(None, None, 0, 1)
+        lib.ctbb_profile_enable(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        lib.ctbb_profile_enable(0)
+        stage_ms = (C.c_double * 5)()
+        stage_n = (C.c_uint64 * 5)()
+        lib.ctbb_profile_read(stage_ms, stage_n, 5, 1)
+    finally:
+        L.call("ctbb_set_storage", L.STORAGE_FP32)
+    ms = e0.elapsed_time(e1) / args.steps
+    diff = (d_out - d_ref).double().abs()
+    hu = 1000.0 / scans.MU_WATER
+    # the filter's tensor work: 3 BF16 products of 2 n^2 FLOP per row over the
+    # union's rows and the edge views' rows
+    n = mr.cg.n_channels_oversampled
+    filter_rows = (sizes["union_rebin_samples"] // n)
+    flop = 3 * 2.0 * n * n * filter_rows
+    ramp_ms = stage_ms[2] / args.steps
+    out = {"value": sizes["vu_total"] / (ms * 1e-3), "unit": "voxel-updates/s", "ms_per_step": ms,
+           "scans_per_s": 1e3 / ms,
+           "stages_ms_per_step": {name: stage_ms[i] / args.steps for i, name in enumerate(STAGES)},
+           "ramp_filter_tensor": {"flop_per_union_pass": flop, "ms_per_step_incl_edge_views": ramp_ms,
+                                  "achieved_tflops_lower_bound": flop / (ramp_ms * 1e-3) / 1e12,
+                                  "note": "BF16 hi/lo products (3 per sample pair) of the union's rows; the "
+                                          "stage time also covers the edge views' rows and the row split"},
+           "max_hu_vs_fp32_path": float(diff.max()) * hu,
+           "rms_hu_vs_fp32_path": float(diff.pow(2).mean().sqrt()) * hu,
+           "entry_point": m["dev_entry"] + " after ctbb_set_storage(CTBB_STORAGE_FP16)"}
+    if ref is not None:
+        out["hu"] = hu_compare(ref, d_out)
+    del d_out
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -826,12 +897,19 @@ def run_ours(args):
         return
 
     # HU errors of the benched output (sampled patches of the middle block)
-    hu = None
+    hu, ref = None, None
     if not args.no_hu:
         try:
-            hu = hu_check(mr, blocks, m["d_scan"], m["d_final"], spec.n_readings)
+            ref = hu_reference(mr, blocks, m["d_scan"], spec.n_readings)
+            hu = hu_compare(ref, m["d_final"])
         except Exception as e:  # reported in the line, the rest of the run stands
             hu = {"error": "%s: %s" % (type(e).__name__, e)}
+    fp16 = None
+    if not args.no_fp16:
+        try:
+            fp16 = measure_fp16(args, torch, lib, m, ref)
+        except Exception as e:
+            fp16 = {"error": "%s: %s" % (type(e).__name__, e)}
     raw0 = None
     if world == 1 and not args.no_cpu_baseline:
         raw0 = window_from_device(m["d_scan"], blocks[0], spec.n_readings, mr.cg.n_rows_raw * mr.cg.n_channels)
@@ -920,6 +998,7 @@ def run_ours(args):
             "parallelism": "replicas" if world > 1 else "single GPU",
         },
         "hu": hu,
+        "fp16_storage": fp16,
         "roofline": {"kernel": "backproject_kernel", "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                      "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 > 0 else None,
                      "traffic": traffic, "flop_per_vu": FLOP_PER_VU, "vu_per_launch": vu_per_launch,

@@ -17,7 +17,7 @@ BUILD = os.path.join(REPO, "_build")
 LIB = os.path.join(HERE, "libctbb_gb300.so")
 
 CUDA_SOURCES = [
-    "abi.cu", "adaptive_filter.cu", "rebin.cu", "ramp_filter.cu",
+    "abi.cu", "adaptive_filter.cu", "rebin.cu", "ramp_filter.cu", "ramp_tc.cu",
     "backproject.cu", "finalize.cu",
 ]
 HOST_SOURCES = ["planner.cpp", "dicom.cpp", "server.cpp"]

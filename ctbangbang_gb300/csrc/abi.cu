@@ -26,6 +26,7 @@
 #include "cuda_util.cuh"
 #include "finalize.h"
 #include "ramp_filter.h"
+#include "ramp_tc.h"
 #include "rebin.h"
 
 namespace ctbb {
@@ -77,6 +78,12 @@ struct Context {
     DeviceBuffer edge_raw;
     DeviceRebinTables rebin_tables;
     RampFilterPlan ramp;
+    RampTcPlan ramp_tc;
+    DeviceBuffer tc_work;
+    // whole-scan row storage: 0 float32 rows, 1 FP16 footprint quads + per-view
+    // scales written by the tensor-core ramp filter (quads, qscale)
+    int storage = 0;
+    DeviceBuffer quads, qscale;
     void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
     int sms = 0;
     std::atomic<int> device{-1};  // the device the work buffers live on (-1: none yet)
@@ -311,6 +318,57 @@ static int do_backproject(Context &c, const struct recon_metadata &mr, const flo
                               d_rebin, d_block, bp_zpt(), c.stream);
 }
 
+// The whole-scan paths' backprojection of one block from the context's rows:
+// float32 rows (c.rebin) or footprint quads (c.quads, c.qscale).
+static int backproject_scan_rows(Context &c, const struct recon_metadata &mr, float *d_block, const ViewRows &rows)
+{
+    if (c.storage == 0) return do_backproject(c, mr, c.rebin.as<float>(), d_block, &rows);
+    BackprojectTables t;
+    CTBB_TRY(build_backproject_tables(mr, &t));
+    for (int i = 0; i < t.n_half; ++i)
+        for (int k = 0; k < t.nht; ++k) t.set_view_row(i, k, rows.row(i + k * t.n_half));
+    CTBB_TRY(upload(c.bp_views, t.views, c.stream));
+    CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
+    CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    StageScope scope(c, 3);
+    return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
+                              reinterpret_cast<const float *>(c.quads.ptr), d_block, 8, c.stream,
+                              c.qscale.as<float>());
+}
+
+// Ramp filter of rows [row0, row0 + n_lines) of the whole-scan rows buffer:
+// float32 in place, or through the tensor cores into the footprint quads and
+// scales at the same row index.
+static int filter_scan_rows(Context &c, size_t row0, size_t n_lines, int rows_per_view, int n_os)
+{
+    StageScope scope(c, 2);
+    if (c.storage == 0)
+        return launch_ramp_filter(c.ramp, c.rebin.as<float>() + row0 * (size_t)n_os, n_lines, c.stream);
+    return launch_ramp_tc(c.ramp_tc, c.rebin.as<float>() + row0 * (size_t)n_os, n_lines,
+                          reinterpret_cast<__half *>(c.quads.ptr) + row0 * (size_t)n_os * 4,
+                          c.qscale.as<float>() + row0, c.tc_work.ptr, c.stream, rows_per_view);
+}
+
+// Buffers and filter plan of the whole-scan paths for rows_total rows of the
+// plan's geometry (the union's rows and the largest edge patch).
+static int prepare_scan_rows(Context &c, const struct recon_metadata &mg, size_t rows_total, size_t union_lines)
+{
+    BlockDims d = block_dims(mg);
+    std::vector<float> taps(2 * d.n_os);
+    CTBB_TRY(ctbb_load_filter(&mg, taps.data()));
+    CTBB_TRY(c.rebin.ensure(rows_total * d.n_os * sizeof(float)));
+    if (c.storage == 0) return prepare_ramp_filter(taps.data(), (int)d.n_os, &c.ramp, c.stream);
+    if (!ramp_tc_supported((int)d.n_os) || d.n_rows == 0 || 128 % d.n_rows != 0) {
+        set_error("FP16 row storage needs rows of a multiple of 64 samples up to 1536 (here %zu) and detector rows "
+                  "dividing 128 (here %zu)", d.n_os, d.n_rows);
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(prepare_ramp_tc(taps.data(), (int)d.n_os, &c.ramp_tc, c.stream));
+    CTBB_TRY(c.quads.ensure(rows_total * d.n_os * 4 * sizeof(__half)));
+    CTBB_TRY(c.qscale.ensure(rows_total * sizeof(float)));
+    return c.tc_work.ensure(ramp_tc_work_bytes(union_lines, (int)d.n_os));
+}
+
 static int do_finalize(Context &c, const struct recon_metadata &mr, const float *d_image, float *d_final, float mu_water)
 {
     FinalizeTables t;
@@ -343,6 +401,23 @@ extern "C" int ctbb_set_stream(void *stream)
 
 extern "C" uint64_t ctbb_kernel_launch_count(void) { return ctx().launches.load(); }
 
+static int set_storage(Context &c, int mode)
+{
+    if (mode != CTBB_STORAGE_FP32 && mode != CTBB_STORAGE_FP16) {
+        set_error("row storage %d is neither CTBB_STORAGE_FP32 nor CTBB_STORAGE_FP16", mode);
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.storage = mode;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_set_storage(int mode)
+{
+    clear_error();
+    return set_storage(ctx(), mode);
+}
+
 // Frees every work buffer, table, copy stream and staging buffer of c, on the
 // device they live on.  device_sync: wait for the whole device first (the
 // default context, whose stream the caller chooses); else for c's streams.
@@ -368,6 +443,10 @@ static void release_context(Context &c, bool device_sync, bool unbind)
     c.rebin_tables = DeviceRebinTables{};
     if (c.ramp.d_spectrum) cudaFree(c.ramp.d_spectrum);
     c.ramp = RampFilterPlan{};
+    release_ramp_tc(&c.ramp_tc);
+    c.tc_work.release();
+    c.quads.release();
+    c.qscale.release();
     if (c.copy_stream) {
         for (int i = 0; i < 2; ++i) {
             cudaEventDestroy(c.copied[i]);
@@ -454,6 +533,33 @@ extern "C" int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os,
     std::lock_guard<std::mutex> lk(c.mu);
     CTBB_TRY(prepare_ramp_filter(h_taps, n_os, &c.ramp, c.stream));
     return launch_ramp_filter(c.ramp, d_lines, n_lines, c.stream);
+}
+
+extern "C" int ctbb_ramp_filter_fp16_device(const float *d_lines, size_t n_lines, int n_os, const float *h_taps,
+                                            int rows_per_view, void *d_out, float *d_scale)
+{
+    clear_error();
+    if (!d_lines || !h_taps || !d_out || !d_scale || n_os <= 0) {
+        set_error("ctbb_ramp_filter_fp16_device: bad argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    if (!ramp_tc_supported(n_os)) {
+        set_error("ctbb_ramp_filter_fp16_device: row length %d is not a multiple of 64 up to 1536", n_os);
+        return CTBB_ERR_ARGUMENT;
+    }
+    if (rows_per_view < 0 || (rows_per_view > 0 && 128 % rows_per_view != 0)) {
+        set_error("ctbb_ramp_filter_fp16_device: rows per view %d must divide 128", rows_per_view);
+        return CTBB_ERR_ARGUMENT;
+    }
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    CTBB_TRY(prepare_ramp_tc(h_taps, n_os, &c.ramp_tc, c.stream));
+    CTBB_TRY(c.tc_work.ensure(ramp_tc_work_bytes(n_lines, n_os)));
+    StageScope scope(c, 2);
+    CTBB_TRY(launch_ramp_tc(c.ramp_tc, d_lines, n_lines, static_cast<__half *>(d_out), d_scale, c.tc_work.ptr,
+                            c.stream, rows_per_view));
+    return ramp_tc_check(c.ramp_tc, c.stream);
 }
 
 extern "C" int ctbb_backproject_device(const struct recon_metadata *mr, const float *d_rebin, float *d_block)
@@ -673,9 +779,10 @@ static void edge_extent(const struct recon_metadata &mr, const std::vector<struc
 // window length differs) into d_patch, and ramp-filtered.
 static int run_edge_patch(Context &c, const struct recon_metadata &mb, const EdgePlan &e, const RebinTables &rt,
                           const float *d_union_raw, const float *d_union_sup, long long g0, float *d_block_scratch,
-                          float *d_patch)
+                          size_t patch_view)
 {
     BlockDims d = block_dims(mb);
+    float *d_patch = c.rebin.as<float>() + patch_view * d.n_rows * d.n_os;
     const size_t frame = d.n_rows_raw * d.n_channels;
     const size_t view_elems = d.n_rows * d.n_os;
     const long long sb = (long long)(int)mb.ri.idx_pull_start - g0;
@@ -695,8 +802,7 @@ static int run_edge_patch(Context &c, const struct recon_metadata &mb, const Edg
             CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(),
                                   d_patch - (size_t)(e.d1 - e.d0) * view_elems, c.stream, e.d1, e.n_used));
     }
-    StageScope scope(c, 2);
-    return launch_ramp_filter(c.ramp, d_patch, (size_t)e.n_patch() * d.n_rows, c.stream);
+    return filter_scan_rows(c, patch_view * d.n_rows, (size_t)e.n_patch() * d.n_rows, (int)d.n_rows, (int)d.n_os);
 }
 
 // Device bytes the whole-scan paths (scan_device / scan_host / scan_file)
@@ -775,8 +881,7 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
             StageScope scope(c, 0);
             CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
         }
-        const size_t view_elems = dg.n_rows * dg.n_os;
-        CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * view_elems) * sizeof(float)));
+        CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
         RebinTables rt;
         CTBB_TRY(build_rebin_tables(mg, &rt));
         rt.split_view_coord = 1;  // the union's frame offsets are large
@@ -785,7 +890,7 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
             StageScope scope(c, 1);
             CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
         }
-        CTBB_TRY(do_filter(c, mg, c.rebin.as<float>()));
+        CTBB_TRY(filter_scan_rows(c, 0, dg.n_views * dg.n_rows, (int)dg.n_rows, (int)dg.n_os));
         if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
         for (size_t b = 0; b < blocks.size(); ++b) {
             mr->ri = blocks[b];
@@ -800,12 +905,13 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
             vr.patch = dg.n_views;
             if (e.any())
                 CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
-                                        c.rebin.as<float>() + dg.n_views * view_elems));
+                                        dg.n_views));
             float *slab = c.image.as<float>() + b * n_block * plane;
-            CTBB_TRY(do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr));
+            CTBB_TRY(backproject_scan_rows(c, *mr, slab, vr));
         }
         CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
         CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        if (c.storage) CTBB_TRY(ramp_tc_check(c.ramp_tc, c.stream));
         return CTBB_OK;
     });
 }
@@ -1043,7 +1149,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
     CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    CTBB_TRY(c.rebin.ensure((dg.rebin_elems() + max_patch * dg.n_rows * dg.n_os) * sizeof(float)));
+    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
     CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
     if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
@@ -1065,14 +1171,10 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     int status = feed.begin(c, g0, g1, chunk, n_chunks, d_raw);
     // per-scan tables, once
     RebinTables rt;
-    std::vector<float> taps(2 * dg.n_os);
     if (status == CTBB_OK) status = build_rebin_tables(mg, &rt);
     rt.split_view_coord = 1;  // the union's frame offsets are large
     if (status == CTBB_OK) status = upload_rebin_tables(rt, &c.rebin_tables, c.stream);
-    if (status == CTBB_OK) status = ctbb_load_filter(&mg, taps.data());
-    if (status == CTBB_OK) status = prepare_ramp_filter(taps.data(), (int)dg.n_os, &c.ramp, c.stream);
     AfStream af(mg);
-    const size_t view_elems = dg.n_rows * dg.n_os;
     const int V = (int)dg.n_views;
     int v_done = 0;
     size_t b_done = 0;
@@ -1103,11 +1205,8 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
                                       v_done, v_ready);
             }
             if (status != CTBB_OK) break;
-            {
-                StageScope scope(c, 2);
-                status = launch_ramp_filter(c.ramp, c.rebin.as<float>() + (size_t)v_done * view_elems,
-                                            (size_t)(v_ready - v_done) * dg.n_rows, c.stream);
-            }
+            status = filter_scan_rows(c, (size_t)v_done * dg.n_rows, (size_t)(v_ready - v_done) * dg.n_rows,
+                                      (int)dg.n_rows, (int)dg.n_os);
             if (status != CTBB_OK) break;
             v_done = v_ready;
         }
@@ -1132,10 +1231,10 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             vr.patch = dg.n_views;
             if (e.any())
                 status = run_edge_patch(c, mb, e, rt, d_raw, c.scratch.as<float>(), g0,
-                                        c.scratch.as<float>() + af_union, c.rebin.as<float>() + dg.n_views * view_elems);
+                                        c.scratch.as<float>() + af_union, dg.n_views);
             if (status != CTBB_OK) break;
             float *slab = c.image.as<float>() + b_done * n_block * plane;
-            status = do_backproject(c, *mr, c.rebin.as<float>(), slab, &vr);
+            status = backproject_scan_rows(c, *mr, slab, vr);
             ++b_done;
         }
     }
@@ -1149,6 +1248,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
     CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
                                   cudaMemcpyDeviceToHost, c.stream));
+    if (c.storage) CTBB_TRY(ramp_tc_check(c.ramp_tc, c.stream));
     CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return CTBB_OK;
 }
@@ -1470,7 +1570,7 @@ static size_t context_device_bytes(const Context &c)
     size_t n = 0;
     for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                                   &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                                  &c.fin_weights, &c.edge_raw})
+                                  &c.fin_weights, &c.edge_raw, &c.tc_work, &c.quads, &c.qscale})
         n += b->bytes;
     return n + c.ramp.capacity * sizeof(float2);
 }
@@ -1516,6 +1616,16 @@ extern "C" int ctbb_context_destroy(ctbb_context h)
     }
     delete h;
     return CTBB_OK;
+}
+
+extern "C" int ctbb_context_set_storage(ctbb_context h, int mode)
+{
+    clear_error();
+    if (!h) {
+        set_error("ctbb_context_set_storage: null context");
+        return CTBB_ERR_ARGUMENT;
+    }
+    return set_storage(h->c, mode);
 }
 
 extern "C" int ctbb_context_set_stream(ctbb_context h, void *stream)

@@ -31,6 +31,7 @@
 // the image sums in shared memory.  The per-view table (theta, sin, cos and
 // the ray term) is built on the host with the reference's float expressions.
 // Samples are gathered through the read-only cache.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -49,7 +50,8 @@ namespace ctbb {
 namespace {
 
 struct BpParams {
-    const float *rebin;    // [V][R][Nos]
+    const float *rebin;    // [V][R][Nos] float32, or footprint quads [V][R][Nos][4] FP16
+    const float *vscale;   // quads: scale of row r of view v at [v R + r] (one per view); else null
     uint64_t rebin_rows;   // address of rebin - kFloorMagicBits rows (mod 2^64): see row_floor
     float *out;            // [n_slices_block][ny][nx]
     const float4 *views;   // [n_half][nht] {row index bits, sin, cos, theta z_rot / 2 pi'}
@@ -145,15 +147,29 @@ __device__ __forceinline__ float2 row_floor(float2 ql)
 // The 2x2 footprint {(p, row), (p+1, row), (p, row+1), (p+1, row+1)} of a
 // view, row in [0, R-2] given as t = kFloorMagic + row (row_floor);
 // `view_rows` is the view's (p, 0) address moved back by kFloorMagicBits rows.
+template <bool QUAD>
 __device__ __forceinline__ void fetch_footprint(uint64_t view_rows, int nos, float t, float &v00, float &v01,
                                                 float &v10, float &v11)
 {
-    const float *r0 = reinterpret_cast<const float *>(
-        view_rows + (uint64_t)__float_as_uint(t) * (uint64_t)((unsigned)nos * sizeof(float)));
-    v00 = __ldg(r0);
-    v01 = __ldg(r0 + 1);
-    v10 = __ldg(r0 + nos);
-    v11 = __ldg(r0 + nos + 1);
+    if constexpr (QUAD) {
+        // footprint quads: the four FP16 samples in one 8-byte word
+        const uint2 *q = reinterpret_cast<const uint2 *>(
+            view_rows + (uint64_t)__float_as_uint(t) * (uint64_t)((unsigned)nos * sizeof(uint2)));
+        const uint2 w = __ldg(q);
+        const float2 top = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
+        const float2 bot = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
+        v00 = top.x;
+        v01 = top.y;
+        v10 = bot.x;
+        v11 = bot.y;
+    } else {
+        const float *r0 = reinterpret_cast<const float *>(
+            view_rows + (uint64_t)__float_as_uint(t) * (uint64_t)((unsigned)nos * sizeof(float)));
+        v00 = __ldg(r0);
+        v01 = __ldg(r0 + 1);
+        v10 = __ldg(r0 + nos);
+        v11 = __ldg(r0 + nos + 1);
+    }
 }
 
 // Packed FP32 pairs (sm_100 family): one instruction for two lanes.
@@ -164,9 +180,10 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 
 // NOS > 0: the row length as a compile-time constant (the second row of a
 // footprint is then an immediate offset); 0: taken from p.nos.
-template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS = 256>
+template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS = 256, bool QUAD = false>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpParams p)
 {
+    constexpr unsigned kElem = QUAD ? sizeof(uint2) : sizeof(float);
     constexpr int SUB = ZPT < kSub ? ZPT : kSub;  // slices per sub-chunk
     const int nos = NOS > 0 ? NOS : p.nos;
     // A CTA covers cta_w x (256 / cta_w) voxel columns; each warp a warp_w x
@@ -278,7 +295,13 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             int ip = p_ok ? (int)p_idx : 0;
             float wp = p_idx - (float)ip;
             const uint64_t view_rows =
-                p.rebin_rows + ((uint64_t)__float_as_uint(t.x) * view_stride + (unsigned)ip) * sizeof(float);
+                p.rebin_rows + ((uint64_t)__float_as_uint(t.x) * view_stride + (unsigned)ip) * kElem;
+            // quads: the view's scale, folded into the weights of its samples
+            float2 vs2 = make_float2(1.0f, 1.0f);
+            if constexpr (QUAD) {
+                const float vs = __ldg(p.vscale + (size_t)__float_as_uint(t.x) * p.n_rows);
+                vs2 = make_float2(vs, vs);
+            }
             // Slices are processed in pairs (z, z + 1) with packed FP32
             // arithmetic (one FFMA2 / FADD2 / FMUL2 per two slices); floors,
             // conversions and loads stay per slice.
@@ -291,8 +314,8 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
             auto pair_value = [&](float2 ql, float2 tr) -> float2 {
                 float2 wq = sub2(ql, sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
                 float a00, a01, a10, a11, b00, b01, b10, b11;
-                fetch_footprint(view_rows, nos, tr.x, a00, a01, a10, a11);
-                fetch_footprint(view_rows, nos, tr.y, b00, b01, b10, b11);
+                fetch_footprint<QUAD>(view_rows, nos, tr.x, a00, a01, a10, a11);
+                fetch_footprint<QUAD>(view_rows, nos, tr.y, b00, b01, b10, b11);
                 float2 c0 = fma2(wp2, make_float2(a01, b01), mul2(omwp2, make_float2(a00, b00)));
                 float2 c1 = fma2(wp2, make_float2(a11, b11), mul2(omwp2, make_float2(a10, b10)));
                 return fma2(wq, sub2(c1, c0), c0);
@@ -330,7 +353,8 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                         for (int mm = 0; mm < SUB / 2; ++mm) {
                             const int m = sc * (SUB / 2) + mm;
                             float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
-                            s2[m] = add2(s2[m], pair_value(ql, row_floor(ql)));
+                            if constexpr (QUAD) s2[m] = fma2(pair_value(ql, row_floor(ql)), vs2, s2[m]);
+                            else s2[m] = add2(s2[m], pair_value(ql, row_floor(ql)));
                         }
                     }
                     ++n_flat[sc];
@@ -346,6 +370,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                             float2 w = pair_weight(q);
                             h2[m] = add2(h2[m], w);
                             float2 ql = fma2(q, hr2, hr2);
+                            if constexpr (QUAD) w = mul2(w, vs2);
                             s2[m] = fma2(w, pair_value(ql, row_floor(ql)), s2[m]);
                         }
                     } else {
@@ -393,7 +418,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                                 ok_y = last_turn_sample_valid(p, x, y, __ldg(p.theta + (size_t)i * p.nht + k), t.y,
                                                               t.z, phat, __ldg(p.zpos + z0 + 2 * m + 1), k);
                         }
-                        s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
+                        float2 wv = make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f);
+                        if constexpr (QUAD) wv = mul2(wv, vs2);
+                        s2[m] = fma2(wv, v, s2[m]);
                     }
                     continue;
                 }
@@ -411,7 +438,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
                     float2 tr = row_floor(ql);
                     tr = make_float2(fminf(fmaxf(tr.x, kFloorMagic), t_max), fminf(fmaxf(tr.y, kFloorMagic), t_max));
                     float2 v = pair_value(ql, tr);
-                    s2[m] = fma2(p_ok ? w : make_float2(0.0f, 0.0f), v, s2[m]);
+                    float2 wv = p_ok ? w : make_float2(0.0f, 0.0f);
+                    if constexpr (QUAD) wv = mul2(wv, vs2);
+                    s2[m] = fma2(wv, v, s2[m]);
                 }
             }
         }
@@ -525,8 +554,9 @@ void BackprojectTables::set_view_row(int i, int k, unsigned row)
 
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
-                       float *d_block, int zpt, cudaStream_t stream)
+                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale)
 {
+    const bool quad = d_vscale != nullptr;
     const struct ct_geom &cg = mr.cg;
     const struct recon_params &rp = mr.rp;
     const float pi = kPiBackproject;
@@ -534,8 +564,9 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
     p.rebin = d_rebin;
     // row_floor's addressing: the base moved back by kFloorMagicBits rows,
     // modulo 2^64 (every row address comes back inside the buffer)
-    p.rebin_rows = (uint64_t)(uintptr_t)d_rebin -
-                   (uint64_t)kFloorMagicBits * (uint64_t)cg.n_channels_oversampled * sizeof(float);
+    p.vscale = d_vscale;
+    p.rebin_rows = (uint64_t)(uintptr_t)d_rebin - (uint64_t)kFloorMagicBits * (uint64_t)cg.n_channels_oversampled *
+                                                      (quad ? sizeof(uint2) : sizeof(float));
     p.out = d_block;
     p.views = d_views;
     p.theta = d_theta;
@@ -619,6 +650,22 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
             backproject_kernel<Z, 3, 0><<<grid, block, 0, stream>>>(p);
         }
     };
+    if (quad) {
+        // footprint quads: the default launch shape only (8 slices per
+        // thread, 128-thread CTAs, 7 per SM)
+        if (threads != 128 || zpt != 8) {
+            p.warp_w = 8;
+            p.cta_w = 64;
+        }
+        dim3 qblock(32, 4);
+        dim3 qgrid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + 128 / p.cta_w - 1) / (128 / p.cta_w), (p.n_slices + 7) / 8);
+        if (p.nos == 1472) backproject_kernel<8, 7, 1472, 128, true><<<qgrid, qblock, 0, stream>>>(p);
+        else if (p.nos == 1344) backproject_kernel<8, 7, 1344, 128, true><<<qgrid, qblock, 0, stream>>>(p);
+        else backproject_kernel<8, 7, 0, 128, true><<<qgrid, qblock, 0, stream>>>(p);
+        count_launch();
+        CTBB_CUDA_TRY(cudaGetLastError());
+        return CTBB_OK;
+    }
     switch (zpt) {
     case 16: go(std::integral_constant<int, 16>()); break;
     case 4: go(std::integral_constant<int, 4>()); break;

@@ -26,6 +26,8 @@ struct BackprojectTables {
 int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables *t);
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
-                       float *d_block, int zpt, cudaStream_t stream);
+                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale = nullptr);
+// d_vscale non-null: d_rebin holds footprint quads [V][R][Nos][4] FP16 (the
+// reduced-storage rows, see ramp_tc.h) with view v's scale at d_vscale[v R].
 
 }  // namespace ctbb

@@ -12,6 +12,8 @@ from .structs import ReconMetadata, ReconParams
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libctbb_gb300.so")
 
+STORAGE_FP32, STORAGE_FP16 = 0, 1
+
 STATUS = {
     0: "CTBB_OK", 1: "CTBB_ERR_ARGUMENT", 2: "CTBB_ERR_CONFIG", 3: "CTBB_ERR_RANGE",
     4: "CTBB_ERR_IO", 5: "CTBB_ERR_CUDA", 6: "CTBB_ERR_NO_DEVICE", 7: "CTBB_ERR_ALLOC",
@@ -45,6 +47,9 @@ PROTOTYPES = {
     "ctbb_adaptive_filter_device_noalloc": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_rebin_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_ramp_filter_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F]),
+    "ctbb_ramp_filter_fp16_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F, C.c_int, _VP, _VP]),
+    "ctbb_set_storage": (C.c_int, [C.c_int]),
+    "ctbb_context_set_storage": (C.c_int, [C.c_void_p, C.c_int]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_scan_workspace_bytes": (C.c_size_t, [_MR]),
     "ctbb_server_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]),

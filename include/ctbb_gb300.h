@@ -333,6 +333,23 @@ int ctbb_rebin_device(const struct recon_metadata *mr, const float *d_raw,
 int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os,
                             const float *h_taps);
 
+/* Ramp filter of n_lines rows of length n_os (a multiple of 64, at most
+   1536) as a Toeplitz contraction on the tensor cores: each product in BF16
+   hi + lo halves (x_hi T_hi + x_hi T_lo + x_lo T_hi), accumulated in FP32.
+   The result is stored as FP16 with a power-of-two scale per row, d_scale
+   [n_lines]: y = stored value * d_scale.  rows_per_view = 0: d_out
+   [n_lines][n_os] FP16 (2 bytes per sample), one scale per row.
+   rows_per_view = R > 0 (R divides 128; lines are views of R detector rows):
+   every row of a view has the view's scale, and d_out [n_lines][n_os][4] FP16
+   holds each sample's bilinear footprint (y[r][c], y[r][c+1], y[r+1][c],
+   y[r+1][c+1]) / scale, zero where r + 1 or c + 1 leaves the view (8 bytes
+   per sample: one load per interpolation in the backprojector).  d_lines
+   (float32, device) is not changed.  The same convolution as the reference's
+   filter (include/rebin_filter.cuh:369-409) and filter_cpu
+   (src/rebin_filter_cpu.cu:647-709); the reduced-storage path's filter. */
+int ctbb_ramp_filter_fp16_device(const float *d_lines, size_t n_lines, int n_os, const float *h_taps,
+                                 int rows_per_view, void *d_out, float *d_scale);
+
 /* Backprojection of one block of filtered rebinned views into
    d_block [n_slices_block][ny][nx] (overwritten). */
 int ctbb_backproject_device(const struct recon_metadata *mr,
@@ -397,6 +414,19 @@ int ctbb_reconstruct_scan_file(struct recon_metadata *mr, float *h_final, float 
 int ctbb_reconstruct_host(struct recon_metadata *mr, const float *h_scan, float *h_final,
                           float mu_water);
 
+/* Row storage of the whole-scan paths (ctbb_reconstruct_scan_*), library-wide
+   context: CTBB_STORAGE_FP32 (default) keeps the ramp-filtered rows in
+   float32 (FFT convolution); CTBB_STORAGE_FP16 filters them on the tensor
+   cores (ctbb_ramp_filter_fp16_device) into FP16 footprint words with one
+   power-of-two scale per view, which the backprojector reads (one 8-byte
+   load per interpolation), all voxel accumulation staying FP32.  FP16 needs
+   rows of a multiple of 64 samples up to 1536 and detector rows dividing 128
+   (else the reconstruction returns CTBB_ERR_ARGUMENT).  No counterpart in the
+   reference, which keeps float32 rows. */
+#define CTBB_STORAGE_FP32 0
+#define CTBB_STORAGE_FP16 1
+int ctbb_set_storage(int mode);
+
 /* Per-stage device timing with CUDA events on the library stream.
    Stages: 0 adaptive filter, 1 rebin, 2 ramp filter, 3 backprojection,
    4 finalize.  ctbb_profile_read synchronises on the recorded events, adds
@@ -436,6 +466,8 @@ int ctbb_context_create(ctbb_context *out);
 int ctbb_context_destroy(ctbb_context ctx);
 /* Issue the context's work on the caller's stream from now on. */
 int ctbb_context_set_stream(ctbb_context ctx, void *stream);
+/* ctbb_set_storage for the context's whole-scan calls. */
+int ctbb_context_set_storage(ctbb_context ctx, int mode);
 /* Frees the context's work buffers (kept and reused between calls otherwise). */
 int ctbb_context_release_workspace(ctbb_context ctx);
 /* Device bytes the context's work buffers hold now. */
