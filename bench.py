@@ -69,6 +69,10 @@ def parse_args():
     ap.add_argument("--path", choices=["scan", "blocks"], default="scan",
                     help="scan: one resident rebinned scan for all blocks (ctbb_reconstruct_scan_*); "
                          "blocks: the reference's block loop (ctbb_reconstruct_device / _host)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-scans measurement")
+    ap.add_argument("--batch-scans", type=int, default=24)
+    ap.add_argument("--batch-budget-gb", type=float, default=100.0,
+                    help="device bytes of rows a batch may hold before it runs")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the served-stream measurement (request server vs the plain per-scan path)")
     ap.add_argument("--serve-requests", type=int, default=32)
@@ -858,7 +862,7 @@ def measure_fp16(args, torch, lib, m, ref):
            "stages_ms_per_step": {name: stage_ms[i] / args.steps for i, name in enumerate(STAGES)},
            "ramp_filter_tensor": {"flop_per_union_pass": flop, "ms_per_step_incl_edge_views": ramp_ms,
                                   "achieved_tflops_lower_bound": flop / (ramp_ms * 1e-3) / 1e12,
-                                  "note": "BF16 hi/lo products (3 per sample pair) of the union's rows; the "
+                                  "note": "FP16 hi/lo products (3 per sample pair) of the union's rows; the "
                                           "stage time also covers the edge views' rows and the row split"},
            "max_hu_vs_fp32_path": float(diff.max()) * hu,
            "rms_hu_vs_fp32_path": float(diff.pow(2).mean().sqrt()) * hu,
@@ -963,6 +967,13 @@ def run_ours(args):
             beside = {"error": "%s: %s" % (type(e).__name__, e)}
         torch.cuda.empty_cache()
 
+    batch = None
+    if world == 1 and not args.no_batch:
+        try:
+            batch = batch_measure(args, torch)
+        except Exception as e:
+            batch = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
     serve = None
     if world == 1 and not args.no_serve:
         try:
@@ -1012,6 +1023,7 @@ def run_ours(args):
         "other_path": m["other_path"],
         "e2e_file": m.get("e2e_file"),
         "beside": beside,
+        "batch": batch,
         "serve": serve,
         "gpu_launches": m["launches"] / args.steps,
         "clocks": m["clocks"],
@@ -1050,6 +1062,117 @@ def serve_spec(rng, i, full):
         spec.n_slices = int(spec.n_slices * 0.85)
     spec.turns = max(float(turns), scans.needed_turns(spec))
     return spec
+
+
+BATCH_CONFIG = 4  # the batched workload: scan i is seeded 1000 * 4 + i
+
+
+def batch_measure(args, torch):
+    """Batched uneven scans: `batch_scans` seeded scans of the full batched
+    distribution (serve_spec with full ranges: rotations 2-30, pitch 0.6-1.5,
+    FFS none/phi/z/both, 16/32/64 rows, field 250-500 mm, 256^2 or 512^2,
+    20-300 slices, I0 2e4-2e5).  Plain: each scan alone through
+    ctbb_reconstruct_scan_device (float32 rows, default launch shape), one
+    after another.  Batched: ctbb_batch_begin / _add_device / _run with the
+    autotuner's launch shapes, in float32 and in FP16 storage; scans are added
+    until their rows would pass the batch memory budget, then the batch runs.
+    Times are CUDA events around the library calls (the synthetic scans are
+    projected outside them); every batched stack is compared with its scan
+    alone."""
+    from ctbangbang_gb300 import lib as L
+    from ctbangbang_gb300 import scans
+    lib = L.load()
+    rng = np.random.default_rng(1000 * BATCH_CONFIG)
+    tmp = tempfile.TemporaryDirectory(prefix="ctbb_batch_")
+    specs, mrs, finals, vus = [], [], [], []
+    for i in range(args.batch_scans):
+        spec = serve_spec(rng, i, True)
+        spec.seed = 1000 * BATCH_CONFIG + i
+        mr = scans.plan_spec(spec, os.path.join(tmp.name, str(i)))
+        specs.append(spec)
+        mrs.append(mr)
+        finals.append(lib.ctbb_n_slices_final(C.byref(mr)) * mr.rp.nx * mr.rp.ny)
+        vus.append(workload_sizes(mr, block_plans(mr))["vu_total"])
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        a, b = ev(), ev()
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    # plain: each scan alone (one warm-up call for the first, whose buffers
+    # then cover the sizes that follow only as they grow)
+    alone, t_plain = [], []
+    for k in range(len(specs)):
+        d = ctbb_synth.project_scan_device(torch, mrs[k], specs[k])
+        out = torch.empty(finals[k], dtype=torch.float32, device="cuda")
+        call = lambda: L.call("ctbb_reconstruct_scan_device", C.byref(mrs[k]), C.c_void_p(d.data_ptr()),
+                              C.c_void_p(out.data_ptr()), C.c_float(0.0))
+        call()
+        t_plain.append(timed(call))
+        alone.append(out.cpu())
+        del d, out
+    lib.ctbb_release_workspace()
+    torch.cuda.empty_cache()
+    plain_ms = sum(t_plain)
+    hu = 1000.0 / scans.MU_WATER
+    results = {}
+    for storage, mode in (("fp32", L.STORAGE_FP32), ("fp16", L.STORAGE_FP16)):
+        L.call("ctbb_set_storage", mode)
+        budget = args.batch_budget_gb * (1 << 30)
+        row_bytes = 4 if mode == L.STORAGE_FP32 else 12  # float32 rows, or float32 rows + FP16 quads
+        outs = [torch.empty(finals[k], dtype=torch.float32, device="cuda") for k in range(len(specs))]
+        total_ms, runs, held = 0.0, 0, 0
+        try:
+            for rep in range(2):  # the first pass tunes and sizes the slots; the second is timed
+                total_ms, runs, held = 0.0, 0, 0
+                L.call("ctbb_batch_begin")
+                for k in range(len(specs)):
+                    need = lib.ctbb_scan_workspace_bytes(C.byref(mrs[k]))
+                    if held and held + need * row_bytes // 8 > budget:
+                        total_ms += timed(lambda: L.call("ctbb_batch_run"))
+                        runs += 1
+                        held = 0
+                        L.call("ctbb_batch_begin")
+                    d = ctbb_synth.project_scan_device(torch, mrs[k], specs[k])
+                    total_ms += timed(lambda: L.call("ctbb_batch_add_device", C.byref(mrs[k]),
+                                                     C.c_void_p(d.data_ptr()), C.c_void_p(outs[k].data_ptr()),
+                                                     C.c_float(0.0)))
+                    held += need * row_bytes // 8
+                    del d
+                total_ms += timed(lambda: L.call("ctbb_batch_run"))
+                runs += 1
+        finally:
+            L.call("ctbb_set_storage", L.STORAGE_FP32)
+        diffs = [((outs[k].cpu().double() - alone[k].double()).abs()) for k in range(len(specs))]
+        results[storage] = {
+            "scans_per_s": len(specs) / (total_ms * 1e-3), "ms_total": total_ms, "batch_runs": runs,
+            "vs_plain": plain_ms / total_ms,
+            "max_hu_vs_alone_fp32": max(float(d.max()) for d in diffs) * hu,
+            "rms_hu_vs_alone_fp32": float(np.sqrt(np.mean([float(d.pow(2).mean()) for d in diffs]))) * hu}
+        del outs
+        lib.ctbb_release_workspace()
+        torch.cuda.empty_cache()
+    buf = C.create_string_buffer(1 << 16)
+    lib.ctbb_autotune_report(buf, len(buf))
+    for mr in mrs:
+        scans.free_plan(mr)
+    desc = ["%s rows %d, %.1f rot, pitch %.2f, %d^2, %d slices, fov %.0f" % (
+        {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(s.z_ffs, s.phi_ffs)],
+        s.n_rows, s.turns, s.pitch, s.nx, s.n_slices, s.recon_fov) for s in specs]
+    return {
+        "workload": "%d seeded scans of the batched distribution (rotations 2-30, pitch 0.6-1.5, FFS "
+                    "none/phi/z/both, 16/32/64 rows, 250-500 mm, 256^2 or 512^2, 20-300 slices)" % len(specs),
+        "scans": desc, "voxel_updates": sum(vus),
+        "plain_scans_per_s": len(specs) / (plain_ms * 1e-3), "plain_ms_total": plain_ms,
+        "batched": results,
+        "autotune": buf.value.decode(errors="replace").splitlines(),
+        "entry_points": "ctbb_batch_begin / _add_device / _run (autotuned shapes) vs ctbb_reconstruct_scan_device",
+        "memory_budget_gb": args.batch_budget_gb,
+    }
 
 
 def percentile(v, q):

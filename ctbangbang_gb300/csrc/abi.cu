@@ -15,7 +15,9 @@
 #include <algorithm>
 #include <new>
 #include <condition_variable>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <thread>
 #include <vector>
@@ -84,6 +86,10 @@ struct Context {
     // scales written by the tensor-core ramp filter (quads, qscale)
     int storage = 0;
     DeviceBuffer quads, qscale;
+    // every block's backprojector tables of a prepared whole scan
+    DeviceBuffer bp_tables;
+    // time the backprojector's launch shapes once per geometry class
+    bool autotune = false;
     void *our_d_rebin = nullptr;  // last d_rebin handed out by the drop-in rebin_filter
     int sms = 0;
     std::atomic<int> device{-1};  // the device the work buffers live on (-1: none yet)
@@ -447,6 +453,7 @@ static void release_context(Context &c, bool device_sync, bool unbind)
     c.tc_work.release();
     c.quads.release();
     c.qscale.release();
+    c.bp_tables.release();
     if (c.copy_stream) {
         for (int i = 0; i < 2; ++i) {
             cudaEventDestroy(c.copied[i]);
@@ -472,11 +479,14 @@ static void release_context(Context &c, bool device_sync, bool unbind)
     if (bound >= 0 && bound != cur) cudaSetDevice(cur);
 }
 
+static void release_slots();
+
 extern "C" int ctbb_release_workspace(void)
 {
     Context &c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     release_context(c, true, true);
+    release_slots();
     return CTBB_OK;
 }
 
@@ -758,16 +768,18 @@ static EdgePlan edge_plan(const struct recon_metadata &mb, long long g0, long lo
 
 // Largest pull window and edge patch (views) over the blocks of a plan.
 static void edge_extent(const struct recon_metadata &mr, const std::vector<struct recon_info> &blocks,
-                        long long g0, long long g1, size_t *max_pull, size_t *max_patch)
+                        long long g0, long long g1, size_t *max_pull, size_t *max_patch, size_t *sum_patch = nullptr)
 {
     *max_pull = 0;
     *max_patch = 0;
+    if (sum_patch) *sum_patch = 0;
     for (const auto &ri : blocks) {
         struct recon_metadata mb = mr;
         mb.ri = ri;
         EdgePlan e = edge_plan(mb, g0, g1);
         *max_pull = std::max(*max_pull, (size_t)ri.n_proj_pull);
         *max_patch = std::max(*max_patch, (size_t)e.n_patch());
+        if (sum_patch) *sum_patch += (size_t)e.n_patch();
     }
 }
 
@@ -820,10 +832,10 @@ extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
     BlockDims dg = block_dims(mg);
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     const int n_final = ctbb_n_slices_final(mr);
-    size_t max_pull = 0, max_patch = 0;
-    edge_extent(m, blocks, g0, g1, &max_pull, &max_patch);
+    size_t max_pull = 0, max_patch = 0, sum_patch = 0;
+    edge_extent(m, blocks, g0, g1, &max_pull, &max_patch, &sum_patch);
     const size_t frame = dg.n_rows_raw * dg.n_channels, view_elems = dg.n_rows * dg.n_os;
-    return (2 * dg.raw_elems() + dg.rebin_elems() + max_patch * view_elems + max_pull * frame +
+    return (2 * dg.raw_elems() + dg.rebin_elems() + sum_patch * view_elems + max_pull * frame +
             adaptive_filter_scratch_floats(dg.n_proj_pull) + adaptive_filter_scratch_floats(max_pull) +
             plane * mr->ri.n_slices_recon + plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
            ((size_t)8 << 20);
@@ -837,6 +849,182 @@ extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
 // again for every block).  Differs from the block loop only in the adaptive
 // filter's 18- and 180-degree statistics windows, which here are not cut at
 // the edges of each block's window.
+// A whole scan prepared for its backprojections (prepare_scan_device): the
+// blocks' plans, where each block's views sit in the context's rows, and the
+// offsets of each block's tables (views, theta, slice positions) in
+// c.bp_tables.
+struct ScanPrep {
+    std::vector<struct recon_info> blocks;
+    std::vector<ViewRows> rows;
+    std::vector<BackprojectTables> tables;
+    std::vector<size_t> table_off;  // floats: views (16-byte aligned), then theta, then zpos
+};
+
+// Union window adaptive-filtered, rebinned and ramp-filtered once, every
+// block's edge views re-made into rows of their own after the union's, and
+// every block's tables uploaded, on c's buffers and stream.  The caller holds
+// c.mu.  mr->ri is left at the last block.
+static int prepare_scan_device(Context &c, struct recon_metadata *mr, const float *d_scan, ScanPrep *prep)
+{
+    const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
+    const long long n_readings = (long long)mr->rp.n_readings;
+    const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+    long long g0 = 0, g1 = 0;
+    struct recon_metadata mg;
+    CTBB_TRY(plan_union(mr, &prep->blocks, &g0, &g1, &mg));
+    const std::vector<struct recon_info> &blocks = prep->blocks;
+    BlockDims dg = block_dims(mg);
+    const float *d_win = nullptr;
+    if (g0 >= 0 && g1 <= n_readings) {
+        d_win = d_scan + (size_t)g0 * frame;
+    } else {
+        CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
+        CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, dg.raw_elems() * sizeof(float), c.stream));
+        long long a = g0 < 0 ? 0 : g0, e = g1 > n_readings ? n_readings : g1;
+        if (e > a)
+            CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - g0) * frame, d_scan + (size_t)a * frame,
+                                          (size_t)(e - a) * frame * sizeof(float), cudaMemcpyDeviceToDevice,
+                                          c.stream));
+        d_win = c.raw_in.as<float>();
+    }
+    CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
+    CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
+    size_t max_pull = 0, max_patch = 0, sum_patch = 0;
+    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch, &sum_patch);
+    const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
+    CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
+    {
+        StageScope scope(c, 0);
+        CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
+    }
+    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + sum_patch) * dg.n_rows, dg.n_views * dg.n_rows));
+    RebinTables rt;
+    CTBB_TRY(build_rebin_tables(mg, &rt));
+    rt.split_view_coord = 1;  // the union's frame offsets are large
+    CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
+    {
+        StageScope scope(c, 1);
+        CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
+    }
+    CTBB_TRY(filter_scan_rows(c, 0, dg.n_views * dg.n_rows, (int)dg.n_rows, (int)dg.n_os));
+    if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
+    // every block's edge views in rows of their own, and its tables
+    prep->rows.assign(blocks.size(), ViewRows{});
+    prep->tables.assign(blocks.size(), BackprojectTables{});
+    prep->table_off.assign(blocks.size(), 0);
+    std::vector<float> host_tables;
+    size_t patch_view = dg.n_views;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        mr->ri = blocks[b];
+        ViewRows &vr = prep->rows[b];
+        vr.off = union_view_offset(blocks[b], g0);
+        EdgePlan e = edge_plan(*mr, g0, g1);
+        vr.d0 = e.d0;
+        vr.d1 = e.d1;
+        vr.n_used = e.n_used;
+        vr.patch = patch_view;
+        if (e.any())
+            CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
+                                    patch_view));
+        patch_view += (size_t)e.n_patch();
+        BackprojectTables &t = prep->tables[b];
+        CTBB_TRY(build_backproject_tables(*mr, &t));
+        for (int i = 0; i < t.n_half; ++i)
+            for (int k = 0; k < t.nht; ++k) t.set_view_row(i, k, vr.row(i + k * t.n_half));
+        size_t off = (host_tables.size() + 3) & ~(size_t)3;
+        prep->table_off[b] = off;
+        host_tables.resize(off);
+        host_tables.insert(host_tables.end(), t.views.begin(), t.views.end());
+        host_tables.insert(host_tables.end(), t.theta.begin(), t.theta.end());
+        host_tables.insert(host_tables.end(), t.zpos.begin(), t.zpos.end());
+    }
+    return upload(c.bp_tables, host_tables, c.stream);
+}
+
+// Kernel parameters of block b of a prepared scan (its image slab d_block).
+static int prepared_block_params(Context &c, const struct recon_metadata &mb, const ScanPrep &prep, size_t b,
+                                 float *d_block, const BpShape &shape, BpParams *p)
+{
+    const BackprojectTables &t = prep.tables[b];
+    const float *base = c.bp_tables.as<float>() + prep.table_off[b];
+    const float4 *d_views = reinterpret_cast<const float4 *>(base);
+    const float *d_theta = base + t.views.size();
+    const float *d_zpos = d_theta + t.theta.size();
+    const float *rows = c.storage ? reinterpret_cast<const float *>(c.quads.ptr) : c.rebin.as<float>();
+    const float *vscale = c.storage ? c.qscale.as<float>() : nullptr;
+    return make_backproject_params(mb, t, d_views, d_theta, d_zpos, rows, d_block, vscale, shape, p);
+}
+
+// ---- autotuner -------------------------------------------------------------
+// Picks a backprojector launch shape (slices per thread, CTA size, CTAs per
+// SM, CTA width) for each geometry class -- image size, slices per block, row
+// length, detector rows, half turns, row storage -- by timing every candidate
+// once on the first block of that class (CUDA events on the context's
+// stream; the block is recomputed by the chosen shape afterwards), and caches
+// the choice for the process.
+
+struct TuneKey {
+    int nx, ny, n_slices, nos, n_rows, nht, quad;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(nx, ny, n_slices, nos, n_rows, nht, quad) <
+               std::tie(o.nx, o.ny, o.n_slices, o.nos, o.n_rows, o.nht, o.quad);
+    }
+};
+
+struct TuneEntry {
+    BpShape shape;
+    double ms[8] = {0};  // candidate times, in backproject_shape_candidates order
+    int n = 0;
+};
+
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneEntry> g_tuned;
+
+static int tuned_shape(Context &c, const BpParams &p_any, const BpShape &fallback, BpShape *out)
+{
+    const bool quad = p_any.vscale != nullptr;
+    const TuneKey key{p_any.nx, p_any.ny, p_any.n_slices, p_any.nos, p_any.n_rows, p_any.nht, quad ? 1 : 0};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            *out = it->second.shape;
+            return CTBB_OK;
+        }
+    }
+    std::vector<BpShape> cand = backproject_shape_candidates(quad);
+    TuneEntry best;
+    best.shape = fallback;
+    double best_ms = 1e30;
+    cudaEvent_t e0 = pooled_event(c), e1 = pooled_event(c);
+    for (size_t k = 0; k < cand.size() && k < 8; ++k) {
+        BpParams p = p_any;
+        p.warp_w = cand[k].warp_w;
+        p.cta_w = std::max(cand[k].cta_w, p.warp_w);
+        if (cand[k].threads / p.cta_w < 32 / p.warp_w) p.cta_w = (cand[k].threads / 32) * p.warp_w;
+        CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));  // warm-up (module load, caches)
+        CTBB_CUDA_TRY(cudaEventRecord(e0, c.stream));
+        CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));
+        CTBB_CUDA_TRY(cudaEventRecord(e1, c.stream));
+        CTBB_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        CTBB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        best.ms[k] = ms;
+        best.n = (int)k + 1;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.shape = cand[k];
+        }
+    }
+    c.event_pool.push_back(e0);
+    c.event_pool.push_back(e1);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best;
+    *out = best.shape;
+    return CTBB_OK;
+}
+
 static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, const float *d_scan, float *d_final,
                                             float mu_water)
 {
@@ -849,71 +1037,212 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
     CTBB_TRY(require_device(c));
     std::lock_guard<std::mutex> lk(c.mu);
     return drained(c, [&]() -> int {
-        const size_t frame = mr->cg.n_rows_raw * mr->cg.n_channels;
-        const long long n_readings = (long long)mr->rp.n_readings;
         const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
         const size_t n_block = mr->ri.n_slices_block;
-        std::vector<struct recon_info> blocks;
-        long long g0 = 0, g1 = 0;
-        struct recon_metadata mg;
-        CTBB_TRY(plan_union(mr, &blocks, &g0, &g1, &mg));
-        BlockDims dg = block_dims(mg);
-        const float *d_win = nullptr;
-        if (g0 >= 0 && g1 <= n_readings) {
-            d_win = d_scan + (size_t)g0 * frame;
-        } else {
-            CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
-            CTBB_CUDA_TRY(cudaMemsetAsync(c.raw_in.ptr, 0, dg.raw_elems() * sizeof(float), c.stream));
-            long long a = g0 < 0 ? 0 : g0, e = g1 > n_readings ? n_readings : g1;
-            if (e > a)
-                CTBB_CUDA_TRY(cudaMemcpyAsync(c.raw_in.as<float>() + (size_t)(a - g0) * frame, d_scan + (size_t)a * frame,
-                                              (size_t)(e - a) * frame * sizeof(float), cudaMemcpyDeviceToDevice,
-                                              c.stream));
-            d_win = c.raw_in.as<float>();
-        }
-        CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
-        CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-        size_t max_pull = 0, max_patch = 0;
-        edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
-        const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
-        CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
-        {
-            StageScope scope(c, 0);
-            CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
-        }
-        CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
-        RebinTables rt;
-        CTBB_TRY(build_rebin_tables(mg, &rt));
-        rt.split_view_coord = 1;  // the union's frame offsets are large
-        CTBB_TRY(upload_rebin_tables(rt, &c.rebin_tables, c.stream));
-        {
-            StageScope scope(c, 1);
-            CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
-        }
-        CTBB_TRY(filter_scan_rows(c, 0, dg.n_views * dg.n_rows, (int)dg.n_rows, (int)dg.n_os));
-        if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
-        for (size_t b = 0; b < blocks.size(); ++b) {
-            mr->ri = blocks[b];
-            // view j of block b is view j + (pull_start_b - g0) / n_ffs of the
-            // union, except its edge views, re-made after the union's rows
-            ViewRows vr;
-            vr.off = union_view_offset(blocks[b], g0);
-            EdgePlan e = edge_plan(*mr, g0, g1);
-            vr.d0 = e.d0;
-            vr.d1 = e.d1;
-            vr.n_used = e.n_used;
-            vr.patch = dg.n_views;
-            if (e.any())
-                CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
-                                        dg.n_views));
+        ScanPrep prep;
+        CTBB_TRY(prepare_scan_device(c, mr, d_scan, &prep));
+        const BpShape fallback = c.storage ? BpShape{} : default_bp_shape(bp_zpt());
+        for (size_t b = 0; b < prep.blocks.size(); ++b) {
+            mr->ri = prep.blocks[b];
             float *slab = c.image.as<float>() + b * n_block * plane;
-            CTBB_TRY(backproject_scan_rows(c, *mr, slab, vr));
+            BpParams p;
+            CTBB_TRY(prepared_block_params(c, *mr, prep, b, slab, fallback, &p));
+            BpShape shape = fallback;
+            if (c.autotune) {
+                CTBB_TRY(tuned_shape(c, p, fallback, &shape));
+                CTBB_TRY(prepared_block_params(c, *mr, prep, b, slab, shape, &p));
+            }
+            StageScope scope(c, 3);
+            CTBB_TRY(launch_backproject_params(p, shape, c.stream));
         }
         CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
         CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
         if (c.storage) CTBB_TRY(ramp_tc_check(c.ramp_tc, c.stream));
         return CTBB_OK;
     });
+}
+
+// ---- many whole scans, one backprojection launch ---------------------------
+// Every scan of a batch is prepared (union filtered, rebinned, ramp-filtered,
+// edge views re-made, tables uploaded) into a slot of its own -- rows, tables,
+// image -- and then the blocks of all scans are backprojected together: one
+// launch per launch shape (the autotuner's choice for each geometry class),
+// whose CTAs run over the tiles of every block in turn, so the small blocks of
+// short scans fill the GPU beside one another instead of one launch (and one
+// tail) each.  Each scan is then finalized.  The work buffers that the
+// preparation needs only while it runs (raw window, filtered window,
+// statistics) are shared by the slots.
+
+struct ScanSlot {
+    DeviceBuffer rebin, quads, qscale, image, bp_tables;
+    ScanPrep prep;
+};
+
+static std::vector<ScanSlot> g_slots;  // the library-wide context's batch slots (its lock)
+static DeviceBuffer g_batch_params;
+
+static void swap_slot(Context &c, ScanSlot &sl)
+{
+    // with FP16 storage the float32 rows are only the filter's input, used
+    // while the scan is prepared: one buffer serves every slot
+    if (c.storage == 0) std::swap(c.rebin, sl.rebin);
+    std::swap(c.quads, sl.quads);
+    std::swap(c.qscale, sl.qscale);
+    std::swap(c.image, sl.image);
+    std::swap(c.bp_tables, sl.bp_tables);
+}
+
+static void release_slots()
+{
+    for (ScanSlot &sl : g_slots) {
+        for (DeviceBuffer *b : {&sl.rebin, &sl.quads, &sl.qscale, &sl.image, &sl.bp_tables}) b->release();
+    }
+    g_slots.clear();
+    g_batch_params.release();
+}
+
+struct BatchEntry {
+    struct recon_metadata *mr;
+    float *d_final;
+    float mu_water;
+};
+static std::vector<BatchEntry> g_batch;  // scans added since ctbb_batch_begin (the context's lock)
+static std::vector<std::pair<BpShape, BpParams>> g_batch_items;
+
+extern "C" int ctbb_batch_begin(void)
+{
+    clear_error();
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    g_batch.clear();
+    g_batch_items.clear();
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_batch_add_device(struct recon_metadata *mr, const float *d_scan, float *d_final, float mu_water)
+{
+    clear_error();
+    if (!mr || !d_scan || !d_final || !mr->table_positions) {
+        set_error("ctbb_batch_add_device: metadata not configured or null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(check_mr(mr));
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return drained(c, [&]() -> int {
+        const size_t s = g_batch.size();
+        if (g_slots.size() <= s) g_slots.resize(s + 1);
+        ScanSlot &sl = g_slots[s];
+        swap_slot(c, sl);
+        int st = prepare_scan_device(c, mr, d_scan, &sl.prep);
+        const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
+        const BpShape fallback = c.storage ? BpShape{} : default_bp_shape(8);
+        std::vector<std::pair<BpShape, BpParams>> items;
+        for (size_t b = 0; st == CTBB_OK && b < sl.prep.blocks.size(); ++b) {
+            mr->ri = sl.prep.blocks[b];
+            float *slab = c.image.as<float>() + b * mr->ri.n_slices_block * plane;
+            BpParams p;
+            BpShape shape = fallback;
+            st = prepared_block_params(c, *mr, sl.prep, b, slab, fallback, &p);
+            if (st == CTBB_OK) st = tuned_shape(c, p, fallback, &shape);
+            if (st == CTBB_OK) st = prepared_block_params(c, *mr, sl.prep, b, slab, shape, &p);
+            if (st == CTBB_OK) items.push_back({shape, p});
+        }
+        swap_slot(c, sl);
+        if (st != CTBB_OK) return st;
+        g_batch_items.insert(g_batch_items.end(), items.begin(), items.end());
+        g_batch.push_back({mr, d_final, mu_water});
+        return CTBB_OK;  // drained: d_scan is read to the end when this returns
+    });
+}
+
+extern "C" int ctbb_batch_run(void)
+{
+    clear_error();
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    return drained(c, [&]() -> int {
+        std::vector<BpShape> shapes;
+        for (const auto &it : g_batch_items)
+            if (std::find(shapes.begin(), shapes.end(), it.first) == shapes.end()) shapes.push_back(it.first);
+        for (const BpShape &sh : shapes) {
+            std::vector<BpParams> group;
+            for (const auto &it : g_batch_items)
+                if (it.first == sh) group.push_back(it.second);
+            CTBB_TRY(g_batch_params.ensure(backproject_batch_bytes(group.size())));
+            StageScope scope(c, 3);
+            CTBB_TRY(launch_backproject_batch(group, sh, g_batch_params.ptr, g_batch_params.bytes, c.stream));
+        }
+        for (size_t s = 0; s < g_batch.size(); ++s)
+            CTBB_TRY(do_finalize(c, *g_batch[s].mr, g_slots[s].image.as<float>(), g_batch[s].d_final,
+                                 g_batch[s].mu_water));
+        CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        if (c.storage) CTBB_TRY(ramp_tc_check(c.ramp_tc, c.stream));
+        g_batch.clear();
+        g_batch_items.clear();
+        return CTBB_OK;
+    });
+}
+
+extern "C" int ctbb_reconstruct_batch_device(int n_scans, struct recon_metadata *const *mrs,
+                                             const float *const *d_scans, float *const *d_finals, float mu_water)
+{
+    clear_error();
+    if (n_scans <= 0 || !mrs || !d_scans || !d_finals) {
+        set_error("ctbb_reconstruct_batch_device: bad argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    CTBB_TRY(ctbb_batch_begin());
+    for (int s = 0; s < n_scans; ++s) {
+        int st = ctbb_batch_add_device(mrs[s], d_scans[s], d_finals[s], mu_water);
+        if (st != CTBB_OK) {
+            std::string err = ctbb_last_error();
+            ctbb_batch_begin();
+            set_error("scan %d: %s", s, err.c_str());
+            return st;
+        }
+    }
+    return ctbb_batch_run();
+}
+
+extern "C" int ctbb_set_autotune(int on)
+{
+    clear_error();
+    Context &c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.autotune = on != 0;
+    return CTBB_OK;
+}
+
+extern "C" int ctbb_autotune_report(char *buf, size_t n)
+{
+    std::string out;
+    std::vector<BpShape> cq = backproject_shape_candidates(false), cqq = backproject_shape_candidates(true);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto &kv : g_tuned) {
+        const TuneKey &k = kv.first;
+        const TuneEntry &e = kv.second;
+        char line[512];
+        int len = snprintf(line, sizeof(line), "%dx%dx%d nos %d rows %d nht %d %s: zpt %d threads %d ctas/sm %d cta_w %d;",
+                           k.nx, k.ny, k.n_slices, k.nos, k.n_rows, k.nht, k.quad ? "fp16" : "fp32", e.shape.zpt,
+                           e.shape.threads, e.shape.min_blocks, e.shape.cta_w);
+        out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
+        const std::vector<BpShape> &cc = k.quad ? cqq : cq;
+        for (int i = 0; i < e.n && i < (int)cc.size(); ++i) {
+            len = snprintf(line, sizeof(line), " %d/%d/%d/%d %.3f ms", cc[i].zpt, cc[i].threads, cc[i].min_blocks,
+                           cc[i].cta_w, e.ms[i]);
+            out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
+        }
+        out += "\n";
+    }
+    if (buf && n) {
+        size_t m = std::min(n - 1, out.size());
+        std::memcpy(buf, out.data(), m);
+        buf[m] = 0;
+    }
+    return (int)out.size();
 }
 
 extern "C" int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan, float *d_final,
@@ -1570,7 +1899,7 @@ static size_t context_device_bytes(const Context &c)
     size_t n = 0;
     for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                                   &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                                  &c.fin_weights, &c.edge_raw, &c.tc_work, &c.quads, &c.qscale})
+                                  &c.fin_weights, &c.edge_raw, &c.tc_work, &c.quads, &c.qscale, &c.bp_tables})
         n += b->bytes;
     return n + c.ramp.capacity * sizeof(float2);
 }

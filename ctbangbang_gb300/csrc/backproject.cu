@@ -49,34 +49,6 @@ namespace ctbb {
 
 namespace {
 
-struct BpParams {
-    const float *rebin;    // [V][R][Nos] float32, or footprint quads [V][R][Nos][4] FP16
-    const float *vscale;   // quads: scale of row r of view v at [v R + r] (one per view); else null
-    uint64_t rebin_rows;   // address of rebin - kFloorMagicBits rows (mod 2^64): see row_floor
-    float *out;            // [n_slices_block][ny][nx]
-    const float4 *views;   // [n_half][nht] {row index bits, sin, cos, theta z_rot / 2 pi'}
-    const float *theta;    // [n_half][nht] theta (the last-turn border recheck)
-    const float *zpos;     // [n_slices_block]
-    int nx, ny, n_slices, nos, n_rows, nht, n_half;
-    float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
-    float ds_half;         // r_f fai / 2
-    float inv_ds_half;     // 1 / ds_half
-    float two_cc;          // 2 * central channel
-    float coll;            // slice spacing
-    float rf, inv_rf, rf2; // r_f, 1 / r_f, r_f^2
-    float z_rot, two_pi;   // z_rot, 2 pi'
-    float zrot_over_2pi;
-    float tan_cone;
-    int k_window;          // half-turn window per angle (z_rot != 0)
-    int warp_w;            // voxel columns along x per warp (32, 16, 8 or 4)
-    int cta_w;             // voxel columns along x per CTA (a multiple of warp_w)
-    float abs_zr;          // |z_rot / (2 pi')|
-    float inv_half_feed;   // 2 / z_rot: half turns per mm of ray travel
-    float half_rows;       // (R - 1) / 2
-    float taper_scale;     // (pi'/2) / (1 - Q)
-    float out_scale;       // 2 pi' / n_proj_turn
-    int flat_path;         // R >= 8: rows of |q| <= Q never reach a border
-};
 
 constexpr float kQ = 0.6f;
 // slices per sub-chunk: the unit of the flat / inner / other decision
@@ -180,8 +152,11 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 
 // NOS > 0: the row length as a compile-time constant (the second row of a
 // footprint is then an immediate offset); 0: taken from p.nos.
-template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS = 256, bool QUAD = false>
-__global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpParams p)
+// One CTA tile (bx, by, bz) of a block's backprojection with the parameters
+// p (kernel parameters, or a block's entry of a batch copied to shared
+// memory).
+template <int ZPT, int NOS, int THREADS, bool QUAD, class Params>
+__device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by, int bz)
 {
     constexpr unsigned kElem = QUAD ? sizeof(uint2) : sizeof(float);
     constexpr int SUB = ZPT < kSub ? ZPT : kSub;  // slices per sub-chunk
@@ -191,9 +166,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
     // samples lie (a row of 32 columns spreads over up to ~110 channels).
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tiles_x = p.cta_w / p.warp_w;
-    int xi = blockIdx.x * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
-    int yi = blockIdx.y * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
-    int z0 = blockIdx.z * ZPT;
+    int xi = bx * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
+    int yi = by * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
+    int z0 = bz * ZPT;
     if (xi >= p.nx || yi >= p.ny) return;
     // voxel centre with the reference's float operations (no contraction)
     float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
@@ -464,6 +439,49 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
         }
 }
 
+template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS = 256, bool QUAD = false>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpParams p)
+{
+    backproject_tile<ZPT, NOS, THREADS, QUAD>(p, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// The blocks of a batch -- blocks of any number of scans -- in one launch:
+// grid.x runs over the CTA tiles of every block in turn (tile_start[b] is the
+// first tile of block b, tile_start[n_blocks] the total); a CTA finds its
+// block, copies the block's parameters to shared memory and runs its tile.
+template <int ZPT, int MIN_BLOCKS, int NOS, int THREADS, bool QUAD>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
+    backproject_batch_kernel(const BpParams *__restrict__ params, const unsigned *__restrict__ tile_start,
+                             int n_blocks)
+{
+    __shared__ BpParams sp;
+    __shared__ int s_block;
+    const unsigned tile = blockIdx.x;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        int lo = 0, hi = n_blocks - 1;  // the last b with tile_start[b] <= tile
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(tile_start + mid) <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        s_block = lo;
+    }
+    __syncthreads();
+    const int b = s_block;
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(params + b);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+        for (int w = tid; w < (int)(sizeof(BpParams) / 4); w += THREADS) dst[w] = __ldg(src + w);
+    }
+    __syncthreads();
+    const unsigned local = tile - __ldg(tile_start + b);
+    const int cta_h = THREADS / sp.cta_w;
+    const unsigned gx = (unsigned)((sp.nx + sp.cta_w - 1) / sp.cta_w);
+    const unsigned gy = (unsigned)((sp.ny + cta_h - 1) / cta_h);
+    backproject_tile<ZPT, NOS, THREADS, QUAD>(sp, (int)(local % gx), (int)((local / gx) % gy), (int)(local / (gx * gy)));
+}
+
 // Threads (voxel columns) per CTA of the backprojector: 256 or 128.
 int bp_cta_threads()
 {
@@ -552,19 +570,20 @@ void BackprojectTables::set_view_row(int i, int k, unsigned row)
     std::memcpy(&views[((size_t)i * nht + k) * 4], &bits, sizeof(bits));
 }
 
-int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
-                       const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
-                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale)
+int make_backproject_params(const struct recon_metadata &mr, const BackprojectTables &t, const float4 *d_views,
+                            const float *d_theta, const float *d_zpos, const float *d_rebin, float *d_block,
+                            const float *d_vscale, const BpShape &shape, BpParams *pp)
 {
     const bool quad = d_vscale != nullptr;
     const struct ct_geom &cg = mr.cg;
     const struct recon_params &rp = mr.rp;
     const float pi = kPiBackproject;
-    BpParams p;
+    BpParams &p = *pp;
+    std::memset(&p, 0, sizeof(p));
     p.rebin = d_rebin;
+    p.vscale = d_vscale;
     // row_floor's addressing: the base moved back by kFloorMagicBits rows,
     // modulo 2^64 (every row address comes back inside the buffer)
-    p.vscale = d_vscale;
     p.rebin_rows = (uint64_t)(uintptr_t)d_rebin - (uint64_t)kFloorMagicBits * (uint64_t)cg.n_channels_oversampled *
                                                       (quad ? sizeof(uint2) : sizeof(float));
     p.out = d_block;
@@ -609,71 +628,166 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
         set_error("backproject: detector too small");
         return CTBB_ERR_ARGUMENT;
     }
-    const int threads = zpt == 8 ? bp_cta_threads() : 256;
-    p.warp_w = bp_warp_width();
-    p.cta_w = std::max(bp_cta_width(), p.warp_w);
-    if (threads / p.cta_w < 32 / p.warp_w) p.cta_w = (threads / 32) * p.warp_w;  // whole warp tiles in y
-    const int cta_h = threads / p.cta_w;
-    dim3 block(32, threads / 32);
-    dim3 grid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + cta_h - 1) / cta_h, 1);
-    auto go = [&](auto zpt_tag) {
-        constexpr int Z = decltype(zpt_tag)::value;
-        grid.z = (p.n_slices + Z - 1) / Z;
-        // 8 slices: 4 CTAs per SM by default (64 registers), 3 on request;
-        // 16 slices: 3 CTAs (80 registers); the row lengths of the built-in
-        // scanners with flying focal spot get a compile-time row stride
-        // the kernel for the row length in hand: compile-time strides only for
-        // the row lengths they were compiled for, the runtime stride otherwise
-        auto launch = [&](auto mb_tag, auto threads_tag) {
-            constexpr int MB = decltype(mb_tag)::value;
-            constexpr int T = decltype(threads_tag)::value;
-            if (p.nos == 1472) backproject_kernel<Z, MB, 1472, T><<<grid, block, 0, stream>>>(p);
-            else if (p.nos == 1344) backproject_kernel<Z, MB, 1344, T><<<grid, block, 0, stream>>>(p);
-            else backproject_kernel<Z, MB, 0, T><<<grid, block, 0, stream>>>(p);
-        };
-        using T128 = std::integral_constant<int, 128>;
-        using T256 = std::integral_constant<int, 256>;
-        if constexpr (Z == 8) {
-            if (threads == 128) {
-                // 128-thread CTAs: 7 per SM (72 registers) by default, or 8 (64)
-                if (bp_min_blocks() == 8) launch(std::integral_constant<int, 8>(), T128());
-                else launch(std::integral_constant<int, 7>(), T128());
-            } else if (bp_min_blocks() == 3) {
-                launch(std::integral_constant<int, 3>(), T256());
-            } else {
-                launch(std::integral_constant<int, 4>(), T256());
-            }
-        } else if constexpr (Z == 16) {
-            if (bp_min_blocks() == 2) launch(std::integral_constant<int, 2>(), T256());
-            else launch(std::integral_constant<int, 3>(), T256());
-        } else {
-            backproject_kernel<Z, 3, 0><<<grid, block, 0, stream>>>(p);
-        }
-    };
+    p.warp_w = shape.warp_w;
+    p.cta_w = std::max(shape.cta_w, p.warp_w);
+    if (shape.threads / p.cta_w < 32 / p.warp_w) p.cta_w = (shape.threads / 32) * p.warp_w;  // whole warp tiles in y
+    return CTBB_OK;
+}
+
+namespace {
+
+dim3 grid_of(const BpParams &p, const BpShape &s)
+{
+    const int cta_h = s.threads / p.cta_w;
+    return dim3((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + cta_h - 1) / cta_h, (p.n_slices + s.zpt - 1) / s.zpt);
+}
+
+// Calls f(Z, MB, T, QUAD) with the compile-time instance of a launch shape;
+// CTBB_ERR_ARGUMENT for a shape no kernel was compiled for.  batch: the
+// instances the batch kernel is compiled for (a subset).
+template <class F>
+int with_shape(const BpShape &s, bool quad, bool batch, F &&f)
+{
+    using std::integral_constant;
+    auto I = [](auto v) { return v; };
+    (void)I;
     if (quad) {
-        // footprint quads: the default launch shape only (8 slices per
-        // thread, 128-thread CTAs, 7 per SM)
-        if (threads != 128 || zpt != 8) {
-            p.warp_w = 8;
-            p.cta_w = 64;
-        }
-        dim3 qblock(32, 4);
-        dim3 qgrid((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + 128 / p.cta_w - 1) / (128 / p.cta_w), (p.n_slices + 7) / 8);
-        if (p.nos == 1472) backproject_kernel<8, 7, 1472, 128, true><<<qgrid, qblock, 0, stream>>>(p);
-        else if (p.nos == 1344) backproject_kernel<8, 7, 1344, 128, true><<<qgrid, qblock, 0, stream>>>(p);
-        else backproject_kernel<8, 7, 0, 128, true><<<qgrid, qblock, 0, stream>>>(p);
-        count_launch();
-        CTBB_CUDA_TRY(cudaGetLastError());
+        if (s.zpt == 8 && s.threads == 128 && s.min_blocks == 7)
+            return f(integral_constant<int, 8>(), integral_constant<int, 7>(), integral_constant<int, 128>(),
+                     std::true_type());
+    } else if (s.zpt == 8 && s.threads == 128 && s.min_blocks == 7) {
+        return f(integral_constant<int, 8>(), integral_constant<int, 7>(), integral_constant<int, 128>(),
+                 std::false_type());
+    } else if (s.zpt == 8 && s.threads == 256 && s.min_blocks == 4) {
+        return f(integral_constant<int, 8>(), integral_constant<int, 4>(), integral_constant<int, 256>(),
+                 std::false_type());
+    } else if (s.zpt == 16 && s.threads == 256 && s.min_blocks == 3) {
+        return f(integral_constant<int, 16>(), integral_constant<int, 3>(), integral_constant<int, 256>(),
+                 std::false_type());
+    } else if (!batch) {
+        if (s.zpt == 8 && s.threads == 128 && s.min_blocks == 8)
+            return f(integral_constant<int, 8>(), integral_constant<int, 8>(), integral_constant<int, 128>(),
+                     std::false_type());
+        if (s.zpt == 8 && s.threads == 256 && s.min_blocks == 3)
+            return f(integral_constant<int, 8>(), integral_constant<int, 3>(), integral_constant<int, 256>(),
+                     std::false_type());
+        if (s.zpt == 16 && s.threads == 256 && s.min_blocks == 2)
+            return f(integral_constant<int, 16>(), integral_constant<int, 2>(), integral_constant<int, 256>(),
+                     std::false_type());
+        if (s.zpt == 4 && s.threads == 256 && s.min_blocks == 3)
+            return f(integral_constant<int, 4>(), integral_constant<int, 3>(), integral_constant<int, 256>(),
+                     std::false_type());
+    }
+    set_error("backproject: no kernel for %d slices per thread, %d threads, %d CTAs per SM%s%s", s.zpt, s.threads,
+              s.min_blocks, quad ? " (FP16 footprint rows)" : "", batch ? " (batch)" : "");
+    return CTBB_ERR_ARGUMENT;
+}
+
+}  // namespace
+
+BpShape default_bp_shape(int zpt)
+{
+    BpShape s;
+    s.zpt = (zpt == 4 || zpt == 16) ? zpt : 8;
+    s.threads = s.zpt == 8 ? bp_cta_threads() : 256;
+    if (s.zpt == 8) s.min_blocks = s.threads == 128 ? (bp_min_blocks() == 8 ? 8 : 7) : (bp_min_blocks() == 3 ? 3 : 4);
+    else s.min_blocks = (s.zpt == 16 && bp_min_blocks() == 2) ? 2 : 3;
+    s.cta_w = bp_cta_width();
+    s.warp_w = bp_warp_width();
+    return s;
+}
+
+int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream)
+{
+    const bool quad = p.vscale != nullptr;
+    const dim3 grid = grid_of(p, shape);
+    const dim3 block(32, shape.threads / 32);
+    CTBB_TRY(with_shape(shape, quad, false, [&](auto z, auto mb, auto t, auto q) -> int {
+        constexpr int Z = decltype(z)::value, MB = decltype(mb)::value, T = decltype(t)::value;
+        constexpr bool Q = decltype(q)::value;
+        if (p.nos == 1472) backproject_kernel<Z, MB, 1472, T, Q><<<grid, block, 0, stream>>>(p);
+        else if (p.nos == 1344) backproject_kernel<Z, MB, 1344, T, Q><<<grid, block, 0, stream>>>(p);
+        else backproject_kernel<Z, MB, 0, T, Q><<<grid, block, 0, stream>>>(p);
         return CTBB_OK;
-    }
-    switch (zpt) {
-    case 16: go(std::integral_constant<int, 16>()); break;
-    case 4: go(std::integral_constant<int, 4>()); break;
-    default: go(std::integral_constant<int, 8>()); break;
-    }
+    }));
     count_launch();
     CTBB_CUDA_TRY(cudaGetLastError());
     return CTBB_OK;
+}
+
+int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
+                       const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
+                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale, const BpShape *shape)
+{
+    BpShape s = shape ? *shape : default_bp_shape(zpt);
+    if (d_vscale && !shape) s = BpShape{};  // FP16 footprint rows: the default shape
+    BpParams p;
+    CTBB_TRY(make_backproject_params(mr, t, d_views, d_theta, d_zpos, d_rebin, d_block, d_vscale, s, &p));
+    return launch_backproject_params(p, s, stream);
+}
+
+size_t backproject_batch_bytes(size_t n_blocks) { return n_blocks * sizeof(BpParams) + (n_blocks + 1) * 4 + 256; }
+
+int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape &shape, void *d_buf, size_t buf_bytes,
+                             cudaStream_t stream)
+{
+    if (blocks.empty()) return CTBB_OK;
+    const bool quad = blocks[0].vscale != nullptr;
+    for (const BpParams &p : blocks)
+        if ((p.vscale != nullptr) != quad || p.nos != blocks[0].nos) {
+            set_error("backproject batch: blocks of different row storage or row length");
+            return CTBB_ERR_ARGUMENT;
+        }
+    if (backproject_batch_bytes(blocks.size()) > buf_bytes) {
+        set_error("backproject batch: parameter buffer too small");
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::vector<unsigned> start(blocks.size() + 1, 0);
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        dim3 g = grid_of(blocks[b], shape);
+        unsigned long long next = (unsigned long long)start[b] + (unsigned long long)g.x * g.y * g.z;
+        if (next >= (1ull << 31)) {
+            set_error("backproject batch: more than 2^31 CTA tiles");
+            return CTBB_ERR_ARGUMENT;
+        }
+        start[b + 1] = (unsigned)next;
+    }
+    BpParams *d_params = static_cast<BpParams *>(d_buf);
+    unsigned *d_start = reinterpret_cast<unsigned *>(d_params + blocks.size());
+    CTBB_CUDA_TRY(cudaMemcpyAsync(d_params, blocks.data(), blocks.size() * sizeof(BpParams), cudaMemcpyHostToDevice,
+                                  stream));
+    CTBB_CUDA_TRY(cudaMemcpyAsync(d_start, start.data(), start.size() * sizeof(unsigned), cudaMemcpyHostToDevice,
+                                  stream));
+    const unsigned total = start.back();
+    const dim3 block(32, shape.threads / 32);
+    const int nos = blocks[0].nos, n = (int)blocks.size();
+    CTBB_TRY(with_shape(shape, quad, true, [&](auto z, auto mb, auto t, auto q) -> int {
+        constexpr int Z = decltype(z)::value, MB = decltype(mb)::value, T = decltype(t)::value;
+        constexpr bool Q = decltype(q)::value;
+        if (nos == 1472) backproject_batch_kernel<Z, MB, 1472, T, Q><<<total, block, 0, stream>>>(d_params, d_start, n);
+        else backproject_batch_kernel<Z, MB, 0, T, Q><<<total, block, 0, stream>>>(d_params, d_start, n);
+        return CTBB_OK;
+    }));
+    count_launch();
+    CTBB_CUDA_TRY(cudaGetLastError());
+    // the host vectors above are copied from pageable memory: the copies are
+    // staged before cudaMemcpyAsync returns
+    return CTBB_OK;
+}
+
+std::vector<BpShape> backproject_shape_candidates(bool quad)
+{
+    std::vector<BpShape> c;
+    if (quad) {
+        for (int w : {64, 32, 128}) c.push_back(BpShape{8, 128, 7, w, 8});
+        return c;
+    }
+    c.push_back(BpShape{8, 128, 7, 64, 8});
+    c.push_back(BpShape{8, 128, 7, 32, 8});
+    c.push_back(BpShape{8, 128, 7, 128, 8});
+    c.push_back(BpShape{8, 256, 4, 64, 8});
+    c.push_back(BpShape{16, 256, 3, 64, 8});
+    return c;
 }
 
 }  // namespace ctbb

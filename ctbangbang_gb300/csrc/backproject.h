@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <vector>
 
 #include "ctbb_internal.h"
@@ -23,10 +24,66 @@ struct BackprojectTables {
     void set_view_row(int i, int k, unsigned row);
 };
 
+// Kernel parameters of one block's backprojection.
+struct BpParams {
+    const float *rebin;    // [V][R][Nos] float32, or footprint quads [V][R][Nos][4] FP16
+    const float *vscale;   // quads: scale of row r of view v at [v R + r] (one per view); else null
+    uint64_t rebin_rows;   // address of rebin - kFloorMagicBits rows (mod 2^64): see row_floor
+    float *out;            // [n_slices_block][ny][nx]
+    const float4 *views;   // [n_half][nht] {row index bits, sin, cos, theta z_rot / 2 pi'}
+    const float *theta;    // [n_half][nht] theta (the last-turn border recheck)
+    const float *zpos;     // [n_slices_block]
+    int nx, ny, n_slices, nos, n_rows, nht, n_half;
+    float pix_x, pix_y, x_c, y_c, x0, y0;  // x = pix_x * (xi - x_c) + x0
+    float ds_half;         // r_f fai / 2
+    float inv_ds_half;     // 1 / ds_half
+    float two_cc;          // 2 * central channel
+    float coll;            // slice spacing
+    float rf, inv_rf, rf2; // r_f, 1 / r_f, r_f^2
+    float z_rot, two_pi;   // z_rot, 2 pi'
+    float zrot_over_2pi;
+    float tan_cone;
+    int k_window;          // half-turn window per angle (z_rot != 0)
+    int warp_w;            // voxel columns along x per warp (32, 16, 8 or 4)
+    int cta_w;             // voxel columns along x per CTA (a multiple of warp_w)
+    float abs_zr;          // |z_rot / (2 pi')|
+    float inv_half_feed;   // 2 / z_rot: half turns per mm of ray travel
+    float half_rows;       // (R - 1) / 2
+    float taper_scale;     // (pi'/2) / (1 - Q)
+    float out_scale;       // 2 pi' / n_proj_turn
+    int flat_path;         // R >= 8: rows of |q| <= Q never reach a border
+};
+
+// A launch shape: slices per thread, threads per CTA, CTAs per SM the kernel
+// is compiled for, voxel columns along x per CTA and per warp.
+struct BpShape {
+    int zpt = 8, threads = 128, min_blocks = 7, cta_w = 64, warp_w = 8;
+    bool operator==(const BpShape &o) const
+    {
+        return zpt == o.zpt && threads == o.threads && min_blocks == o.min_blocks && cta_w == o.cta_w &&
+               warp_w == o.warp_w;
+    }
+};
+// The shape the environment knobs (CTBB_BP_*) name for this slice count.
+BpShape default_bp_shape(int zpt);
+// Shapes the autotuner times (those the batch kernel is compiled for).
+std::vector<BpShape> backproject_shape_candidates(bool quad);
+
 int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables *t);
+int make_backproject_params(const struct recon_metadata &mr, const BackprojectTables &t, const float4 *d_views,
+                            const float *d_theta, const float *d_zpos, const float *d_rebin, float *d_block,
+                            const float *d_vscale, const BpShape &shape, BpParams *p);
+int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream);
+// Device bytes launch_backproject_batch needs for n blocks' parameters.
+size_t backproject_batch_bytes(size_t n_blocks);
+// All blocks (of any scans; one row storage and row length) in one launch of
+// the given shape; d_buf holds backproject_batch_bytes(blocks.size()).
+int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape &shape, void *d_buf,
+                             size_t buf_bytes, cudaStream_t stream);
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
-                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale = nullptr);
+                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale = nullptr,
+                       const BpShape *shape = nullptr);
 // d_vscale non-null: d_rebin holds footprint quads [V][R][Nos][4] FP16 (the
 // reduced-storage rows, see ramp_tc.h) with view v's scale at d_vscale[v R].
 

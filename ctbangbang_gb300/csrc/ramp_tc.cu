@@ -10,22 +10,31 @@
 // Y = X T.  Here it runs as one GEMM per launch on the 5th-generation tensor
 // cores:
 //
-//   * precision: X and T are split into BF16 pairs, x = x_hi + x_lo with
-//     x_hi = bf16(x), x_lo = bf16(x - x_hi) (16 significant bits together),
-//     and Y = X_hi T_hi + X_hi T_lo + X_lo T_hi, accumulated in FP32 in tensor
-//     memory (the dropped X_lo T_lo term is 2^-16 of the products);
+//   * precision: X and T are split into 16-bit hi + lo pairs, x = x_hi + x_lo
+//     with x_hi = h(x), x_lo = h(x - x_hi), and Y = X_hi T_hi + X_hi T_lo +
+//     X_lo T_hi, accumulated in FP32 in tensor memory.  The halves are FP16
+//     (11 significant bits each, 22 together), not BF16 (8 + 8): the ramp
+//     filter's output is a near-cancellation of terms as large as f[n] x, and
+//     with BF16 halves the residual of x times that centre tap alone left 3e-4
+//     of the row maximum (CPU emulation with exact accumulation: 4.9e-5
+//     absolute on 0.15-maximum rows, against 8e-7 with FP16 halves at the
+//     same tensor-core rate).  FP16's exponent range is narrower (5 bits
+//     against 8), so X is scaled per row (per view) by a power of two to a
+//     maximum of 2^13-2^14 and T by 2^10 (its far taps stay normal); both
+//     scales are exact and undone in the epilogue;
 //   * tiles: a CTA owns 128 rows x 256 output samples (TMEM 128 lanes x 256
 //     FP32 columns); the K loop runs over 64-sample slices of the row (23 for
 //     n = 1472), each one stage of a 2-stage shared-memory ring holding
-//     X_hi, X_lo (128 x 64) and T_hi, T_lo (256 x 64), all BF16, loaded by
+//     X_hi, X_lo (128 x 64) and T_hi, T_lo (256 x 64), all FP16, loaded by
 //     TMA (cp.async.bulk.tensor) with the 128-byte swizzle the MMA
 //     descriptors name; one thread issues 3 x 4 tcgen05.mma (M128 N256 K16)
 //     per stage and tcgen05.commit frees the stage;
-//   * epilogue: the four warps read their 32 TMEM lanes (tcgen05.ld), scale
-//     each row by 2^-e_row and store FP16.  The exponent comes from the row's
-//     input: |y| <= max|x| sum|f|, and 2^e_row is the smallest power of two
-//     putting that bound below 2^14, so no row overflows FP16 and the scale is
-//     exact; the backprojector multiplies by 2^e_row again.
+//   * epilogue: the four warps read their 32 TMEM lanes (tcgen05.ld), undo
+//     the input scales, scale each row by 2^-e_row and store FP16.  The
+//     exponent comes from the row's input: |y| <= max|x| sum|f|, and 2^e_row is
+//     the smallest power of two putting that bound below 2^14, so no row
+//     overflows FP16 and the scale is exact; the backprojector multiplies by
+//     2^e_row again.
 //
 // The split of X and the row exponents are one pass before the GEMM
 // (ramp_tc_split_kernel).  T (both halves, padded to 1536 output samples) is
@@ -33,7 +42,6 @@
 // that runs out records an error code in device memory, the CTA stops
 // issuing work, frees its tensor memory and returns; the host reads the code.
 #include <cuda.h>
-#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -52,7 +60,7 @@ namespace {
 
 constexpr int BM = 128;            // rows per CTA (TMEM lanes)
 constexpr int BN = 256;            // output samples per CTA (TMEM columns)
-constexpr int BK = 64;             // samples of the row per stage (128 bytes of BF16)
+constexpr int BK = 64;             // samples of the row per stage (128 bytes of FP16)
 constexpr int kStages = 2;
 constexpr int kTileA = BM * BK * 2;  // bytes of one A tile (16 KiB)
 constexpr int kTileB = BN * BK * 2;  // bytes of one B tile (32 KiB)
@@ -88,8 +96,10 @@ __device__ __forceinline__ uint64_t global_ns()
 }
 
 // Bounded wait for the phase with the given parity: false once kWaitNs of
-// wall time (or kWaitLimit polls) have passed without it.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// wall time (or kWaitLimit polls) have passed without it, or as soon as
+// another CTA has recorded a wait that ran out (*error non-zero), so that one
+// failure ends the launch in one wait's time, not one per CTA.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, const int *error)
 {
     uint32_t addr = smem_u32(bar);
     uint64_t t0 = 0;
@@ -103,6 +113,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
             : "memory");
         if (done) return true;
         if ((it & 255) == 0) {
+            if (*reinterpret_cast<const volatile int *>(error)) return false;
             const uint64_t t = global_ns();
             if (it == 0) t0 = t;
             else if (t - t0 > kWaitNs) return false;
@@ -119,7 +130,7 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major BF16 tile whose rows are 128
+// Shared-memory matrix descriptor of a K-major 16-bit tile whose rows are 128
 // bytes with the 128-byte swizzle (what TMA writes with SWIZZLE_128B): start
 // address, stride of 8-row groups 1024 bytes, descriptor version 1, layout 2.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
@@ -133,10 +144,10 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
     return d;
 }
 
-// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+// Instruction descriptor of kind::f16: D FP32, A and B FP16, both K-major,
 // N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr int kTapExp = 10;  // T is stored times 2^10
 
 __device__ __forceinline__ void umma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
@@ -169,13 +180,54 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// ---- the split of X: BF16 hi / lo planes and the row exponents -------------
+// ---- the split of X: FP16 hi / lo planes and the row exponents -------------
 
-// One warp per row: max |x| (its exponent bound), then x_hi, x_lo.
+// Exponents of a row (or view) of largest |x| m: the input's, e_in with
+// m 2^-e_in in [2^13, 2^14), and the stored output's, e_out, the smallest
+// with m sum|f| 2^-e_out <= 2^14 (FP16 holds up to 65504).
+__device__ __forceinline__ void row_exponents(float m, float sum_abs_taps, int *e_in, int *e_out)
+{
+    *e_in = 0;
+    *e_out = 0;
+    if (m > 0.0f && isfinite(m)) {
+        int ex;
+        frexpf(m, &ex);          // m = f 2^ex, f in [0.5, 1)
+        *e_in = ex - 14;         // m 2^-e_in in [2^13, 2^14)
+        float bound = m * sum_abs_taps;
+        if (bound > 0.0f && isfinite(bound)) {
+            frexpf(bound / 16384.0f, &ex);
+            *e_out = ex;
+        }
+    }
+    *e_in = max(-120, min(120, *e_in));
+    *e_out = max(-120, min(120, *e_out));
+}
+
+// Scales of a row: scale = 2^e_out (what the backprojector multiplies by) and
+// the epilogue's factor 2^(e_in - 10 - e_out) from the accumulator to the
+// stored value.
+__device__ __forceinline__ void write_row(const float *__restrict__ xr, int n, int lane, int e_in, int e_out,
+                                          __half *__restrict__ hr, __half *__restrict__ lr, float *scale,
+                                          float *mult)
+{
+    if (lane == 0) {
+        *scale = ldexpf(1.0f, e_out);
+        *mult = ldexpf(1.0f, e_in - kTapExp - e_out);
+    }
+    const float s = ldexpf(1.0f, -e_in);
+    for (int i = lane; i < n; i += 32) {
+        float v = xr[i] * s;  // exact: a power of two
+        __half h = __float2half_rn(v);
+        hr[i] = h;
+        lr[i] = __float2half_rn(v - __half2float(h));
+    }
+}
+
+// One warp per row: max |x|, its exponents, then x_hi, x_lo.
 __global__ void __launch_bounds__(256) ramp_tc_split_kernel(const float *__restrict__ x, size_t n_lines, int n,
-                                                            float sum_abs_taps, __nv_bfloat16 *__restrict__ hi,
-                                                            __nv_bfloat16 *__restrict__ lo, float *__restrict__ scale,
-                                                            float *__restrict__ inv_scale)
+                                                            float sum_abs_taps, __half *__restrict__ hi,
+                                                            __half *__restrict__ lo, float *__restrict__ scale,
+                                                            float *__restrict__ mult)
 {
     const int lane = threadIdx.x & 31;
     size_t warp = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
@@ -185,37 +237,18 @@ __global__ void __launch_bounds__(256) ramp_tc_split_kernel(const float *__restr
         float m = 0.0f;
         for (int i = lane; i < n; i += 32) m = fmaxf(m, fabsf(xr[i]));
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        // smallest e with bound * 2^-e <= 2^14; FP16 holds up to 65504
-        float bound = m * sum_abs_taps;
-        int e = 0;
-        if (bound > 0.0f && isfinite(bound)) {
-            int ex;
-            frexpf(bound / 16384.0f, &ex);  // bound / 2^14 = f 2^ex, f in [0.5, 1)
-            e = ex;
-        }
-        e = max(-120, min(120, e));
-        if (lane == 0) {
-            scale[row] = ldexpf(1.0f, e);
-            inv_scale[row] = ldexpf(1.0f, -e);
-        }
-        __nv_bfloat16 *hr = hi + row * (size_t)n, *lr = lo + row * (size_t)n;
-        for (int i = lane; i < n; i += 32) {
-            float v = xr[i];
-            __nv_bfloat16 h = __float2bfloat16_rn(v);
-            hr[i] = h;
-            lr[i] = __float2bfloat16_rn(v - __bfloat162float(h));
-        }
+        int e_in, e_out;
+        row_exponents(m, sum_abs_taps, &e_in, &e_out);
+        write_row(xr, n, lane, e_in, e_out, hi + row * (size_t)n, lo + row * (size_t)n, scale + row, mult + row);
     }
 }
 
 // The same split with one exponent per view: a CTA per view of rpv rows (8
 // warps), the exponent from the largest |x| of all its rows.
 __global__ void __launch_bounds__(256) ramp_tc_split_view_kernel(const float *__restrict__ x, size_t n_lines, int n,
-                                                                 int rpv, float sum_abs_taps,
-                                                                 __nv_bfloat16 *__restrict__ hi,
-                                                                 __nv_bfloat16 *__restrict__ lo,
-                                                                 float *__restrict__ scale,
-                                                                 float *__restrict__ inv_scale)
+                                                                 int rpv, float sum_abs_taps, __half *__restrict__ hi,
+                                                                 __half *__restrict__ lo, float *__restrict__ scale,
+                                                                 float *__restrict__ mult)
 {
     __shared__ float red[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -232,28 +265,11 @@ __global__ void __launch_bounds__(256) ramp_tc_split_view_kernel(const float *__
         m = red[0];
         for (int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
         __syncthreads();
-        float bound = m * sum_abs_taps;
-        int e = 0;
-        if (bound > 0.0f && isfinite(bound)) {
-            int ex;
-            frexpf(bound / 16384.0f, &ex);
-            e = ex;
-        }
-        e = max(-120, min(120, e));
-        for (size_t row = g0 + warp; row < g1; row += 8) {
-            if (lane == 0) {
-                scale[row] = ldexpf(1.0f, e);
-                inv_scale[row] = ldexpf(1.0f, -e);
-            }
-            const float *xr = x + row * (size_t)n;
-            __nv_bfloat16 *hr = hi + row * (size_t)n, *lr = lo + row * (size_t)n;
-            for (int i = lane; i < n; i += 32) {
-                float v = xr[i];
-                __nv_bfloat16 h = __float2bfloat16_rn(v);
-                hr[i] = h;
-                lr[i] = __float2bfloat16_rn(v - __bfloat162float(h));
-            }
-        }
+        int e_in, e_out;
+        row_exponents(m, sum_abs_taps, &e_in, &e_out);
+        for (size_t row = g0 + warp; row < g1; row += 8)
+            write_row(x + row * (size_t)n, n, lane, e_in, e_out, hi + row * (size_t)n, lo + row * (size_t)n,
+                      scale + row, mult + row);
     }
 }
 
@@ -262,9 +278,10 @@ __global__ void __launch_bounds__(256) ramp_tc_split_view_kernel(const float *__
 struct TcParams {
     size_t n_lines;               // rows of X (M)
     int n;                        // row length (K and the valid output samples)
-    const float *inv_scale;       // [n_lines]
+    const float *mult;            // [n_lines]: accumulator -> stored value
     __half *out;                  // [n_lines][n] (plain) or [n_lines][n][4] (footprint quads)
     int *error;                   // non-zero: a bounded wait ran out
+    int rows_per_view;            // footprint quads: detector rows of a view (divides BM)
 };
 
 // Output samples a CTA stores: plain rows all BN it computes; footprint quads
@@ -289,10 +306,37 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
+    // a wait of another CTA ran out: this launch's result is void already
+    // (read once, so that the whole CTA leaves together)
+    __shared__ int s_void;
+    if (threadIdx.x == 0) s_void = *reinterpret_cast<const volatile int *>(p.error);
+    __syncthreads();
+    if (s_void) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_tile = blockIdx.x;               // 256-sample slice of the output
     const size_t m0 = (size_t)blockIdx.y * BM;   // first row
     const int k_tiles = p.n / BK;
+    // K order: the slices of the row farthest from this tile's outputs first.
+    // Near the diagonal the taps are large (the centre tap and its odd
+    // neighbours, which cancel it to a small output); far ones sum to about
+    // 1 % of them.  With the large products last, the FP32 accumulator stays
+    // small for most of its additions, where the tensor cores' accumulation
+    // rounds relative to its magnitude.
+    __shared__ uint8_t k_order[kNPad / BK];
+    if (threadIdx.x == 0) {
+        const int centre2 = 2 * (n_tile * tile_step<QUAD>() + BN / 2);  // twice the centre, in samples
+        for (int i = 0; i < k_tiles; ++i) k_order[i] = (uint8_t)i;
+        for (int i = 0; i < k_tiles; ++i)  // selection sort by distance, descending (k_tiles <= 24)
+            for (int j = i + 1; j < k_tiles; ++j) {
+                const int di = abs(2 * (k_order[i] * BK + BK / 2) - centre2);
+                const int dj = abs(2 * (k_order[j] * BK + BK / 2) - centre2);
+                if (dj > di) {
+                    uint8_t t = k_order[i];
+                    k_order[i] = k_order[j];
+                    k_order[j] = t;
+                }
+            }
+    }
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -317,25 +361,26 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
         // TMA producer
         for (int kt = 0; kt < k_tiles; ++kt) {
             const int s = kt % kStages;
-            if (kt >= kStages && !mbar_wait(&empty[s], ((kt / kStages) - 1) & 1)) {
+            if (kt >= kStages && !mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, p.error)) {
                 atomicExch(p.error, 1);
                 *abort_flag = 1;
                 break;
             }
             if (*abort_flag) break;
             uint8_t *st = smem + s * kStageBytes;
+            const int kx = k_order[kt] * BK;
             mbar_expect_tx(&full[s], kStageBytes);
-            tma_load_2d(st, &map_xh, kt * BK, (int)m0, &full[s]);
-            tma_load_2d(st + kTileA, &map_xl, kt * BK, (int)m0, &full[s]);
-            tma_load_2d(st + 2 * kTileA, &map_th, kt * BK, n_tile * tile_step<QUAD>(), &full[s]);
-            tma_load_2d(st + 2 * kTileA + kTileB, &map_tl, kt * BK, n_tile * tile_step<QUAD>(), &full[s]);
+            tma_load_2d(st, &map_xh, kx, (int)m0, &full[s]);
+            tma_load_2d(st + kTileA, &map_xl, kx, (int)m0, &full[s]);
+            tma_load_2d(st + 2 * kTileA, &map_th, kx, n_tile * tile_step<QUAD>(), &full[s]);
+            tma_load_2d(st + 2 * kTileA + kTileB, &map_tl, kx, n_tile * tile_step<QUAD>(), &full[s]);
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         bool ok = true;
         for (int kt = 0; kt < k_tiles; ++kt) {
             const int s = kt % kStages;
-            if (!mbar_wait(&full[s], (kt / kStages) & 1)) {
+            if (!mbar_wait(&full[s], (kt / kStages) & 1, p.error)) {
                 atomicExch(p.error, 2);
                 *abort_flag = 1;
                 ok = false;
@@ -346,7 +391,7 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
             const uint32_t a_hi = st, a_lo = st + kTileA, b_hi = st + 2 * kTileA, b_lo = st + 2 * kTileA + kTileB;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint32_t off = kk * 32;  // 16 BF16 along K
+                const uint32_t off = kk * 32;  // 16 FP16 along K
                 const uint32_t acc0 = (kt > 0 || kk > 0) ? 1u : 0u;
                 umma(tmem, sw128_desc(a_hi + off), sw128_desc(b_hi + off), acc0);
                 umma(tmem, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
@@ -360,19 +405,20 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
     __syncwarp();
 
     // epilogue: every warp its 32 TMEM lanes (rows)
-    const bool got = mbar_wait(done, 0);
+    const bool got = mbar_wait(done, 0, p.error);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!got && lane == 0) atomicExch(p.error, 3);
     const size_t row = m0 + (size_t)warp * 32 + lane;
     const bool row_ok = got && !*abort_flag && row < p.n_lines;
-    const float inv = row_ok ? __ldg(p.inv_scale + row) : 0.0f;
+    const float inv = row_ok ? __ldg(p.mult + row) : 0.0f;
     if (QUAD) {
         // Footprint quads: the scaled FP16 tile is staged in the (now idle)
         // stage ring, then sample (r, c) is stored with (r, c + 1), (r + 1, c)
         // and (r + 1, c + 1) as one 8-byte word.  The tile's rows are whole
         // views (the rows per view divide 128), so row r + 1 of the tile's
         // last row -- the last detector row of a view, whose footprint the
-        // backprojector never reads -- is stored as zeros.
+        // backprojector never reads -- is stored as zeros, as is row r + 1 of
+        // the last row of every view in the tile.
         constexpr int kLd = BN + 8;  // staged row stride (halves)
         __half *stage = reinterpret_cast<__half *>(smem);
         const bool ok_all = got && !*abort_flag;
@@ -399,7 +445,8 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
                     const int col = c_base + c;
                     if (col >= p.n) break;
                     __half2 top = __halves2half2(s0[c], s0[c + 1]);
-                    __half2 bot = r + 1 < BM ? __halves2half2(s1[c], s1[c + 1]) : __float2half2_rn(0.0f);
+                    __half2 bot = (r + 1) % p.rows_per_view != 0 ? __halves2half2(s1[c], s1[c + 1])
+                                                                  : __float2half2_rn(0.0f);
                     dst[col] = make_uint2(*reinterpret_cast<uint32_t *>(&top), *reinterpret_cast<uint32_t *>(&bot));
                 }
             }
@@ -431,20 +478,40 @@ __global__ void __launch_bounds__(128, 1) ramp_tc_gemm_kernel(const __grid_const
 
 // ---- host ---------------------------------------------------------------------
 
-uint16_t bf16_bits(float f)
+// IEEE binary16 of a finite float, round to nearest even (normal, subnormal
+// and zero results; magnitudes at or above 65520 become infinity).
+uint16_t half_bits(float f)
 {
     uint32_t u;
     std::memcpy(&u, &f, 4);
-    u += 0x7FFFu + ((u >> 16) & 1u);  // round to nearest even (finite values)
-    return (uint16_t)(u >> 16);
+    const uint32_t sign = (u >> 16) & 0x8000u;
+    const float a = std::fabs(f);
+    if (a >= 65520.0f) return (uint16_t)(sign | 0x7C00u);
+    if (a < 6.103515625e-05f) {  // subnormal range: multiples of 2^-24
+        const float q = std::nearbyint(a * 16777216.0f);  // round to nearest even (default mode)
+        return (uint16_t)(sign | (uint32_t)q);
+    }
+    uint32_t m = u & 0x7FFFFFFFu;
+    uint32_t e = (m >> 23) - 127 + 15;
+    uint32_t mant = m & 0x7FFFFFu;
+    uint32_t h = (e << 10) | (mant >> 13);
+    const uint32_t rest = mant & 0x1FFFu;
+    if (rest > 0x1000u || (rest == 0x1000u && (h & 1u))) ++h;  // carries into the exponent as it should
+    return (uint16_t)(sign | h);
 }
 
-float bf16_value(uint16_t b)
+float half_value(uint16_t h)
 {
-    uint32_t u = (uint32_t)b << 16;
-    float f;
-    std::memcpy(&f, &u, 4);
-    return f;
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    const uint32_t e = (h >> 10) & 0x1Fu, mant = h & 0x3FFu;
+    float v;
+    if (e == 0) v = std::ldexp((float)mant, -24);
+    else v = std::ldexp((float)(mant | 0x400u), (int)e - 25);
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    u |= sign;
+    std::memcpy(&v, &u, 4);
+    return v;
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -468,7 +535,7 @@ int encode_fn(EncodeTiled *out)
     return CTBB_OK;
 }
 
-// 2-D BF16 tensor map of a row-major [rows][cols] matrix, box box_rows x 64.
+// 2-D FP16 tensor map of a row-major [rows][cols] matrix, box box_rows x 64.
 int make_map(CUtensorMap *map, const void *base, size_t rows, int cols, int box_rows)
 {
     EncodeTiled enc;
@@ -477,7 +544,7 @@ int make_map(CUtensorMap *map, const void *base, size_t rows, int cols, int box_
     cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
     cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
     cuuint32_t elem[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, elem,
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, elem,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -504,16 +571,25 @@ int prepare_ramp_tc(const float *h_taps, int n, RampTcPlan *plan, cudaStream_t s
     }
     if (plan->n == n && plan->d_t && std::memcmp(plan->taps.data(), h_taps, 2 * n * sizeof(float)) == 0)
         return CTBB_OK;
-    // T^T[l][k] = f[n + l - k] for l < n (zero rows up to 1536), split into BF16 halves
+    // T^T[l][k] = 2^10 f[n + l - k] for l < n (zero rows up to 1536), split
+    // into FP16 halves
     std::vector<uint16_t> th((size_t)kNPad * n, 0), tl((size_t)kNPad * n, 0);
     double sum_abs = 0.0;
-    for (int j = 0; j < 2 * n; ++j) sum_abs += std::fabs((double)h_taps[j]);
+    float max_abs = 0.0f;
+    for (int j = 0; j < 2 * n; ++j) {
+        sum_abs += std::fabs((double)h_taps[j]);
+        max_abs = std::max(max_abs, std::fabs(h_taps[j]));
+    }
+    if (!(max_abs * 1024.0f < 60000.0f)) {
+        set_error("ramp filter (tensor cores): taps up to %g do not fit FP16 after the 2^10 scale", (double)max_abs);
+        return CTBB_ERR_ARGUMENT;
+    }
     for (int l = 0; l < n; ++l)
         for (int k = 0; k < n; ++k) {
-            float f = h_taps[n + l - k];
-            uint16_t h = bf16_bits(f);
+            float f = std::ldexp(h_taps[n + l - k], kTapExp);
+            uint16_t h = half_bits(f);
             th[(size_t)l * n + k] = h;
-            tl[(size_t)l * n + k] = bf16_bits(f - bf16_value(h));
+            tl[(size_t)l * n + k] = half_bits(f - half_value(h));
         }
     if (!plan->d_t) {
         CTBB_CUDA_TRY(cudaMalloc(&plan->d_t, (size_t)2 * kNPad * kNPad * sizeof(uint16_t)));
@@ -543,9 +619,9 @@ int launch_ramp_tc(const RampTcPlan &plan, const float *d_rows, size_t n_lines, 
         set_error("ramp filter (tensor cores): %zu rows exceed the tensor map", n_lines);
         return CTBB_ERR_ARGUMENT;
     }
-    __nv_bfloat16 *xh = static_cast<__nv_bfloat16 *>(d_work);
-    __nv_bfloat16 *xl = xh + n_lines * (size_t)n;
-    float *inv_scale = reinterpret_cast<float *>(xl + n_lines * (size_t)n);
+    __half *xh = static_cast<__half *>(d_work);
+    __half *xl = xh + n_lines * (size_t)n;
+    float *mult = reinterpret_cast<float *>(xl + n_lines * (size_t)n);
     if (rows_per_view > 0 && BM % rows_per_view != 0) {
         set_error("ramp filter (tensor cores): %d rows per view do not divide %d", rows_per_view, BM);
         return CTBB_ERR_ARGUMENT;
@@ -553,11 +629,11 @@ int launch_ramp_tc(const RampTcPlan &plan, const float *d_rows, size_t n_lines, 
     if (rows_per_view > 0) {
         int blocks = (int)std::min<size_t>((n_lines + rows_per_view - 1) / rows_per_view, (size_t)num_sms() * 8);
         ramp_tc_split_view_kernel<<<blocks, 256, 0, stream>>>(d_rows, n_lines, n, rows_per_view, plan.sum_abs_taps,
-                                                              xh, xl, d_scale, inv_scale);
+                                                              xh, xl, d_scale, mult);
     } else {
         int blocks = (int)std::min<size_t>((n_lines + 7) / 8, (size_t)num_sms() * 16);
         ramp_tc_split_kernel<<<blocks, 256, 0, stream>>>(d_rows, n_lines, n, plan.sum_abs_taps, xh, xl, d_scale,
-                                                         inv_scale);
+                                                         mult);
     }
     count_launch();
     CTBB_CUDA_TRY(cudaGetLastError());
@@ -579,9 +655,10 @@ int launch_ramp_tc(const RampTcPlan &plan, const float *d_rows, size_t n_lines, 
     TcParams p;
     p.n_lines = n_lines;
     p.n = n;
-    p.inv_scale = inv_scale;
+    p.mult = mult;
     p.out = d_out;
     p.error = plan.d_error;
+    p.rows_per_view = rows_per_view > 0 ? rows_per_view : BM;
     const int step = quad ? tile_step<true>() : tile_step<false>();
     dim3 grid((n + step - 1) / step, (unsigned)((n_lines + BM - 1) / BM));
     if ((grid.x - 1) * step + BN > kNPad) {

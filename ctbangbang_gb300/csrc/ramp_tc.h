@@ -1,4 +1,4 @@
-// ramp_tc.h -- the ramp filter as a BF16 hi/lo Toeplitz contraction on the
+// ramp_tc.h -- the ramp filter as an FP16 hi/lo Toeplitz contraction on the
 // tensor cores (tcgen05), writing FP16 rows with a per-row power-of-two scale.
 #pragma once
 
@@ -15,7 +15,7 @@ struct RampTcPlan {
     int n = 0;                    // row length
     std::vector<float> taps;      // the 2n taps T was made from
     float sum_abs_taps = 0.0f;    // bound of |y| / max|x|
-    void *d_t = nullptr;          // T^T hi and lo, BF16 [1536][n] each
+    void *d_t = nullptr;          // 2^10 T^T hi and lo, FP16 [1536][n] each
     int *d_error = nullptr;       // set by a pipeline wait that ran out
 };
 

@@ -7,7 +7,9 @@
 // request as soon as the device memory it needs fits the budget next to what
 // the other workers hold, so a request that arrives while others run starts
 // as soon as a slot and memory free up, and its copies and kernels overlap
-// theirs on the GPU.  Each worker keeps its buffers between requests (no
+// theirs on the GPU.  A request that does not fit yet lets the queued requests
+// behind it that do fit start first, until it has waited an age bound (2 s by
+// default); from then on it is served next.  Each worker keeps its buffers between requests (no
 // allocation, so no device-wide synchronisation, in the steady state); when a
 // request does not fit, the worker first drops its own buffers, and idle
 // workers are asked to drop theirs.  A request needing more than the whole
@@ -76,6 +78,8 @@ struct ctbb_server_s {
     Clock::time_point created = Clock::now();
     bool stopping = false;
     int waiters = 0;  // ctbb_server_wait calls in progress
+    double age_bound_ms = 2000.0;  // after this a waiting head request is passed no more
+    uint64_t passed = 0;           // requests started ahead of an older one
     std::vector<Worker> workers;
 };
 
@@ -108,8 +112,22 @@ void worker_main(ctbb_server_s *s, size_t w)
             s->work_cv.wait(lk);
             continue;
         }
-        Job *j = s->queue.front();
+        // The head request, or -- while the head has waited less than the
+        // age bound -- the first queued request that fits beside what the
+        // other workers hold: a large request waiting for memory does not
+        // hold up the small ones behind it, and after the age bound nothing
+        // passes it any more.
         const size_t others = others_bytes(*s, w);
+        size_t pick = 0;
+        const bool head_aged = ms_between(s->queue.front()->submitted, Clock::now()) > s->age_bound_ms;
+        if (!head_aged) {
+            for (size_t q = 0; q < s->queue.size(); ++q)
+                if (others + s->queue[q]->need <= s->budget) {
+                    pick = q;
+                    break;
+                }
+        }
+        Job *j = s->queue[pick];
         bool release_first = false;
         if (others + std::max(me.held, j->need) > s->budget) {
             if (others + j->need <= s->budget) {
@@ -128,7 +146,8 @@ void worker_main(ctbb_server_s *s, size_t w)
                 continue;
             }
         }
-        s->queue.pop_front();
+        s->queue.erase(s->queue.begin() + (long)pick);
+        if (pick) ++s->passed;
         me.busy = true;
         me.reserved = j->need;
         j->started = Clock::now();
@@ -184,6 +203,29 @@ extern "C" int ctbb_server_create(int n_workers, size_t device_budget_bytes, ctb
     for (size_t w = 0; w < s->workers.size(); ++w) s->workers[w].thread = std::thread(worker_main, s, w);
     *out = s;
     return CTBB_OK;
+}
+
+extern "C" int ctbb_server_configure(ctbb_server s, int storage, double age_bound_ms)
+{
+    clear_error();
+    if (!s || !(age_bound_ms >= 0.0)) {
+        set_error("ctbb_server_configure: bad argument");
+        return CTBB_ERR_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Worker &w : s->workers) {
+        int st = ctbb_context_set_storage(w.ctx, storage);
+        if (st != CTBB_OK) return st;
+    }
+    s->age_bound_ms = age_bound_ms;
+    return CTBB_OK;
+}
+
+extern "C" uint64_t ctbb_server_passed_count(ctbb_server s)
+{
+    if (!s) return 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    return s->passed;
 }
 
 extern "C" int ctbb_server_submit(ctbb_server s, struct recon_metadata *mr, const float *h_scan, float *h_final,

@@ -49,6 +49,12 @@ PROTOTYPES = {
     "ctbb_ramp_filter_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F]),
     "ctbb_ramp_filter_fp16_device": (C.c_int, [_VP, C.c_size_t, C.c_int, _F, C.c_int, _VP, _VP]),
     "ctbb_set_storage": (C.c_int, [C.c_int]),
+    "ctbb_reconstruct_batch_device": (C.c_int, [C.c_int, C.POINTER(_MR), C.POINTER(_VP), C.POINTER(_VP), C.c_float]),
+    "ctbb_set_autotune": (C.c_int, [C.c_int]),
+    "ctbb_batch_begin": (C.c_int, []),
+    "ctbb_batch_add_device": (C.c_int, [_MR, _VP, _VP, C.c_float]),
+    "ctbb_batch_run": (C.c_int, []),
+    "ctbb_autotune_report": (C.c_int, [C.c_char_p, C.c_size_t]),
     "ctbb_context_set_storage": (C.c_int, [C.c_void_p, C.c_int]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),
     "ctbb_scan_workspace_bytes": (C.c_size_t, [_MR]),
@@ -56,6 +62,8 @@ PROTOTYPES = {
     "ctbb_server_submit": (C.c_int, [C.c_void_p, _MR, _F, _F, C.c_float, C.POINTER(C.c_uint64)]),
     "ctbb_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, _VP]),
     "ctbb_server_destroy": (C.c_int, [C.c_void_p]),
+    "ctbb_server_configure": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "ctbb_server_passed_count": (C.c_uint64, [C.c_void_p]),
     "ctbb_context_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "ctbb_context_destroy": (C.c_int, [C.c_void_p]),
     "ctbb_context_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -334,8 +334,9 @@ int ctbb_ramp_filter_device(float *d_lines, size_t n_lines, int n_os,
                             const float *h_taps);
 
 /* Ramp filter of n_lines rows of length n_os (a multiple of 64, at most
-   1536) as a Toeplitz contraction on the tensor cores: each product in BF16
-   hi + lo halves (x_hi T_hi + x_hi T_lo + x_lo T_hi), accumulated in FP32.
+   1536) as a Toeplitz contraction on the tensor cores: each product in FP16
+   hi + lo halves (x_hi T_hi + x_hi T_lo + x_lo T_hi, x and T scaled by exact
+   powers of two into FP16's range), accumulated in FP32.
    The result is stored as FP16 with a power-of-two scale per row, d_scale
    [n_lines]: y = stored value * d_scale.  rows_per_view = 0: d_out
    [n_lines][n_os] FP16 (2 bytes per sample), one scale per row.
@@ -384,6 +385,46 @@ int ctbb_reconstruct_device(struct recon_metadata *mr, const float *d_scan,
    data and rebinned rows, one block window and its re-made views. */
 int ctbb_reconstruct_scan_device(struct recon_metadata *mr, const float *d_scan,
                                  float *d_final, float mu_water);
+
+/* Many whole scans at once (no counterpart in the reference, which runs one
+   scan per process): scan s of n_scans -- its own plan mrs[s], raw scan
+   d_scans[s] and final stack d_finals[s], each as for
+   ctbb_reconstruct_scan_device; the scans may differ in every geometry and
+   size -- is filtered, rebinned and ramp-filtered into rows of its own, and
+   then the 32-slice blocks of all scans are backprojected together, in one
+   launch per launch shape, whose CTAs run over the tiles of every block in
+   turn (short scans' small blocks fill the GPU beside one another).  The
+   launch shape of each geometry class (image size, slices per block, row
+   length, detector rows, half turns, row storage) is chosen by the
+   autotuner: every candidate timed once on the first block of the class, the
+   choice kept for the process (ctbb_autotune_report).  Row storage as set by
+   ctbb_set_storage.  Each stack equals its scan's ctbb_reconstruct_scan_device
+   result up to the launch shape's rounding (per-slice sums in another order).
+   Device memory: every scan's rows, tables and image at once, plus one
+   scan's window buffers (kept between calls; ctbb_release_workspace frees
+   them).  mrs[s]->ri is left at the scan's last block. */
+int ctbb_reconstruct_batch_device(int n_scans, struct recon_metadata *const *mrs, const float *const *d_scans,
+                                  float *const *d_finals, float mu_water);
+
+/* The same in steps, so that each raw scan can be freed once it is prepared:
+   ctbb_batch_begin starts an empty batch; ctbb_batch_add_device prepares one
+   scan (as ctbb_reconstruct_scan_device prepares it, into a slot of its own)
+   and returns when d_scan is no longer read; ctbb_batch_run backprojects the
+   blocks of every added scan and writes each final stack.  mr and d_final
+   must stay valid until ctbb_batch_run returns. */
+int ctbb_batch_begin(void);
+int ctbb_batch_add_device(struct recon_metadata *mr, const float *d_scan, float *d_final, float mu_water);
+int ctbb_batch_run(void);
+
+/* on != 0: ctbb_reconstruct_scan_device on the library-wide context also
+   takes the autotuner's launch shape for each block's geometry class (off by
+   default: the measured default shape). */
+int ctbb_set_autotune(int on);
+
+/* The autotuner's choices so far, one text line per geometry class with the
+   time of every candidate shape: writes min(n - 1, length) bytes and a NUL to
+   buf, returns the full length. */
+int ctbb_autotune_report(char *buf, size_t n);
 
 /* ctbb_reconstruct_scan_device from host buffers, streamed (no counterpart in
    the reference): the union window is copied host->device in chunks on a
@@ -492,10 +533,11 @@ int ctbb_context_reconstruct_host(ctbb_context ctx, struct recon_metadata *mr,
 size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr);
 
 /* ---- request server: continuous batching of whole scans -----------------
-   n_workers threads, each with its own context, take requests first in first
-   out; a free worker starts the head request as soon as its device memory
+   n_workers threads, each with its own context, take queued requests; a free
+   worker starts the oldest request whose device memory
    (ctbb_scan_workspace_bytes) fits device_budget_bytes next to what the other
-   workers hold, so requests that arrive while others run are admitted as
+   workers hold (a request passed by younger ones for longer than the age
+   bound of ctbb_server_configure is started before any other), so requests that arrive while others run are admitted as
    slots and memory free up and overlap them on the GPU.  Workers keep their
    buffers between requests; when a request does not fit, a worker drops its
    own buffers and asks idle workers to drop theirs.  Each request runs
@@ -516,6 +558,14 @@ struct ctbb_request_result {
 };
 
 int ctbb_server_create(int n_workers, size_t device_budget_bytes, ctbb_server *out);
+/* Row storage of the workers' reconstructions (CTBB_STORAGE_FP32 or
+   CTBB_STORAGE_FP16, see ctbb_set_storage) and the age bound (ms): a queued
+   request that does not fit the budget yet is passed by later requests that
+   do, until it has waited that long (0: strict first in first out).  Call
+   between requests. */
+int ctbb_server_configure(ctbb_server srv, int storage, double age_bound_ms);
+/* Requests started ahead of an older queued one so far. */
+uint64_t ctbb_server_passed_count(ctbb_server srv);
 /* Queue one scan: mr planned (configure_*; not shared with another request in
    flight), h_scan [n_readings][n_rows_raw][n_channels] (pinned host memory
    lets the copies overlap), h_final [n_slices_final][ny][nx].  A scan needing

@@ -72,6 +72,20 @@ def test_compute_entry_points_fail_loudly_without_gpu(lib, tmp_path):
         assert b"no CUDA device" in lib.ctbb_last_error()
     with pytest.raises(L.CtbbError):
         L.call("ctbb_rebin_filter", C.byref(mr))
+    dummy = C.c_void_p(1 << 20)  # never dereferenced: the device check comes first
+    st = lib.ctbb_batch_add_device(C.byref(mr), dummy, dummy, C.c_float(0.0))
+    assert L.STATUS[st] == "CTBB_ERR_NO_DEVICE", lib.ctbb_last_error()
+    assert L.STATUS[lib.ctbb_batch_run()] == "CTBB_ERR_NO_DEVICE"
+    taps = (C.c_float * 256)()
+    st = lib.ctbb_ramp_filter_fp16_device(dummy, 1, 128, taps, 0, dummy, dummy)
+    assert L.STATUS[st] == "CTBB_ERR_NO_DEVICE"
+    # argument checks come before the device check
+    st = lib.ctbb_ramp_filter_fp16_device(dummy, 1, 100, taps, 0, dummy, dummy)
+    assert L.STATUS[st] == "CTBB_ERR_ARGUMENT" and b"multiple of 64" in lib.ctbb_last_error()
+    st = lib.ctbb_ramp_filter_fp16_device(dummy, 1, 128, taps, 48, dummy, dummy)
+    assert L.STATUS[st] == "CTBB_ERR_ARGUMENT"
+    assert L.STATUS[lib.ctbb_set_storage(3)] == "CTBB_ERR_ARGUMENT"
+    assert lib.ctbb_set_storage(L.STORAGE_FP16) == 0 and lib.ctbb_set_storage(L.STORAGE_FP32) == 0
     h = C.c_void_p()
     assert L.STATUS[lib.ctbb_context_create(C.byref(h))] == "CTBB_ERR_NO_DEVICE" and not h.value
     assert L.STATUS[lib.ctbb_server_create(2, C.c_size_t(1 << 30), C.byref(h))] == "CTBB_ERR_NO_DEVICE"
