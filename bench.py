@@ -25,6 +25,7 @@ python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
 import argparse
 import concurrent.futures as cf
+import dataclasses
 import ctypes as C
 import json
 import math
@@ -75,11 +76,11 @@ def parse_args():
                     help="device bytes of rows a batch may hold before it runs")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the served-stream measurement (request server vs the plain per-scan path)")
-    ap.add_argument("--serve-requests", type=int, default=32)
-    ap.add_argument("--serve-scans", type=int, default=8, help="distinct scans the requests draw from")
+    ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--serve-scans", type=int, default=8,
+                    help="distinct scans of the batched distribution the requests draw from (plus one large scan)")
     ap.add_argument("--serve-workers", type=int, default=3)
-    ap.add_argument("--serve-full", action="store_true",
-                    help="the full size distribution (up to 30 rotations, 300 slices) instead of the capped one")
+    ap.add_argument("--serve-window", type=int, default=16, help="requests in flight at most (output buffers)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one block of the config through each stage once (small case for ncu captures)")
     return ap.parse_args()
@@ -1181,23 +1182,36 @@ def percentile(v, q):
 
 
 def serve_measure(args, torch):
-    """The request server (ctbb_server_*) against the plain per-scan path on
-    the same requests: each request is one of `serve_scans` distinct scans
-    (own plan, own output).  Plain: every request alone through
-    ctbb_reconstruct_scan_host, one after another.  Served: all requests
-    submitted at once to a server of `serve_workers` workers (throughput),
-    then as a Poisson stream (latency); the plain path's latency under the
-    same arrivals is its FIFO queue over the measured per-scan times.  Every
-    served stack must equal its scan's stack alone."""
+    """The served reconstruction stream: `serve_requests` requests (600 by
+    default), each one of `serve_scans` distinct seeded scans of the batched
+    size distribution (serve_spec, full ranges) or, with probability 5 %, a
+    large 40-turn 512^2 x 400-slice scan (the precision workload's geometry).
+    A request server (ctbb_server_*, `serve_workers` workers, each request
+    through ctbb_context_reconstruct_scan_host from pinned host buffers) with a
+    150 GB device budget and out-of-order admission (a request that does not
+    fit lets the ones behind it that do pass, for at most 2 s).
+    Plain: every request alone through ctbb_reconstruct_scan_host, one after
+    another (its per-scan times measured once per distinct scan).
+    Served, saturated: requests submitted as fast as results come back, with at
+    most `serve_window` in flight (throughput).  Served, Poisson: arrivals at a
+    rate between 2 and 20 requests/s (80 % of the saturated throughput,
+    clipped to that range) for latency, against the plain path's first come
+    first served queue under the same arrivals.  Every served stack is checked
+    against its scan's stack alone (the same kernels on the same data: equal
+    bit for bit)."""
     from ctbangbang_gb300 import lib as L
     from ctbangbang_gb300 import scans
     from ctbangbang_gb300.serving import Server
     lib = L.load()
-    rng = np.random.default_rng(1000 * SERVE_CONFIG)
+    rng = np.random.default_rng(1000 * SERVE_CONFIG + 5)
     tmp = tempfile.TemporaryDirectory(prefix="ctbb_serve_")
-    specs, prms, host, finals, vus = [], [], [], [], []
-    for i in range(args.serve_scans):
-        spec = serve_spec(rng, i, args.serve_full)
+    pool = [serve_spec(rng, i, True) for i in range(args.serve_scans)]
+    for i, sp in enumerate(pool):
+        sp.seed = 1000 * 5 + i
+    large = dataclasses.replace(scans.CONFIGS["config3"], name="serve_large", seed=1000 * 5 + 99)
+    pool.append(large)
+    prms, host, finals, vus = [], [], [], []
+    for i, spec in enumerate(pool):
         wd = os.path.join(tmp.name, str(i))
         os.makedirs(wd)
         prm, inst = scans.prepare(spec, wd)
@@ -1207,18 +1221,16 @@ def serve_measure(args, torch):
         h = torch.empty(n * frame, dtype=torch.float32, pin_memory=True)
         h.copy_(d)
         del d
-        n_final = lib.ctbb_n_slices_final(C.byref(mr))
-        specs.append(spec)
         prms.append((prm, inst))
         host.append(h)
-        finals.append(n_final * mr.rp.nx * mr.rp.ny)
+        finals.append(lib.ctbb_n_slices_final(C.byref(mr)) * mr.rp.nx * mr.rp.ny)
         vus.append(workload_sizes(mr, block_plans(mr))["vu_total"])
         scans.free_plan(mr)
     torch.cuda.empty_cache()
     fptr = lambda t: t.numpy().ctypes.data_as(C.POINTER(C.c_float))
-    # plain: each scan alone (one warm-up, one timed run); its stack is the reference
+    # plain: each distinct scan alone (one warm-up, one timed run); its stack is the reference
     alone, t_alone = [], []
-    for k in range(len(specs)):
+    for k in range(len(pool)):
         mr = scans.plan(*prms[k])
         out = torch.empty(finals[k], dtype=torch.float32, pin_memory=True)
         L.call("ctbb_reconstruct_scan_host", C.byref(mr), fptr(host[k]), fptr(out), C.c_float(0.0))
@@ -1227,62 +1239,96 @@ def serve_measure(args, torch):
         t_alone.append((time.perf_counter() - t0) * 1e3)
         alone.append(out)
         scans.free_plan(mr)
-    pick = [int(k) for k in rng.integers(len(specs), size=args.serve_requests)]
+    lib.ctbb_release_workspace()
+    torch.cuda.empty_cache()
+    n_req = args.serve_requests
+    pick = [len(pool) - 1 if rng.uniform() < 0.05 else int(rng.integers(args.serve_scans)) for _ in range(n_req)]
     plain_ms = sum(t_alone[k] for k in pick)
     free, total = torch.cuda.mem_get_info()
-    budget = int(min(150 << 30, 0.8 * free))
+    budget = int(min(150 << 30, 0.85 * free))
+    n_buf = max(args.serve_window, args.serve_workers + 2)
+    bufs = [torch.empty(max(finals), dtype=torch.float32, pin_memory=True) for _ in range(n_buf)]
 
     def run_stream(srv, arrivals):
-        mrs = [scans.plan(*prms[k]) for k in pick]
-        outs = [torch.empty(finals[k], dtype=torch.float32, pin_memory=True) for k in pick]
+        """Submits the requests (at the arrival times, or as buffers free up),
+        waits for each, checks it against its scan alone."""
+        import collections
+        mrs = {}
+        inflight = collections.deque()  # (request, ticket, buffer index)
+        free_bufs = list(range(n_buf))
+        res = [None] * n_req
+        same = True
         t0 = time.perf_counter()
-        tickets = []
+
+        def collect_one():
+            nonlocal same
+            r, t, bi = inflight.popleft()
+            res[r] = srv.wait(t)
+            k = pick[r]
+            same = same and bool(torch.equal(bufs[bi][:finals[k]], alone[k]))
+            scans.free_plan(mrs.pop(r))
+            free_bufs.append(bi)
+
         for r, k in enumerate(pick):
             if arrivals is not None:
                 delay = arrivals[r] - (time.perf_counter() - t0)
+                while delay > 0 and inflight and len(free_bufs) < n_buf:
+                    # keep collecting finished requests while waiting for the next arrival
+                    collect_one()
+                    delay = arrivals[r] - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
-            tickets.append(srv.submit(mrs[r], fptr(host[k]), fptr(outs[r])))
-        res = [srv.wait(t) for t in tickets]
+            while not free_bufs:
+                collect_one()
+            bi = free_bufs.pop()
+            mrs[r] = scans.plan(*prms[k])
+            inflight.append((r, srv.submit(mrs[r], fptr(host[k]), fptr(bufs[bi])), bi))
+        while inflight:
+            collect_one()
         wall = (time.perf_counter() - t0) * 1e3
-        same = all(torch.equal(outs[r], alone[k]) for r, k in enumerate(pick))
-        for m in mrs:
-            scans.free_plan(m)
         return res, wall, same
 
     with Server(args.serve_workers, budget) as srv:
-        run_stream(srv, None)  # workers size their buffers
+        L.call("ctbb_server_configure", srv._h, L.STORAGE_FP32, C.c_double(2000.0))
+        # warm-up: every distinct scan once per worker (the workers size their buffers)
+        saved, n_saved = pick, n_req
+        pick = [k for k in range(len(pool)) for _ in range(args.serve_workers)]
+        n_req = len(pick)
+        run_stream(srv, None)
+        pick, n_req = saved, n_saved
         res_sat, wall_sat, same_sat = run_stream(srv, None)
-        served_rate = len(pick) / (wall_sat * 1e-3)
+        served_rate = n_req / (wall_sat * 1e-3)
         rate = min(20.0, max(2.0, 0.8 * served_rate))
-        gaps = rng.exponential(1.0 / rate, size=len(pick))
+        gaps = rng.exponential(1.0 / rate, size=n_req)
         arrivals = np.cumsum(gaps) - gaps[0]
         res_poi, wall_poi, same_poi = run_stream(srv, arrivals)
+        passed = lib.ctbb_server_passed_count(srv._h)
     lat = [r.latency_ms for r in res_poi]
-    # the plain path under the same arrivals: one scan at a time, first come first served
     done, plain_lat = 0.0, []
     for r, k in enumerate(pick):
         start = max(arrivals[r] * 1e3, done)
         done = start + t_alone[k]
         plain_lat.append(done - arrivals[r] * 1e3)
     vu = sum(vus[k] for k in pick)
-    desc = ["%s rows %d%s, %.1f rot, pitch %.2f, %d^2, %d slices, fov %.0f" % (
-        {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(s.z_ffs, s.phi_ffs)],
-        s.n_rows, "", s.turns, s.pitch, s.nx, s.n_slices, s.recon_fov) for s in specs]
+    desc = ["%s rows %d, %.1f rot, pitch %.2f, %d^2, %d slices, fov %.0f" % (
+        {(0, 0): "no FFS", (0, 1): "phi FFS", (1, 0): "z FFS", (1, 1): "phi+z FFS"}[(sp.z_ffs, sp.phi_ffs)],
+        sp.n_rows, sp.turns, sp.pitch, sp.nx, sp.n_slices, sp.recon_fov) for sp in pool]
     return {
-        "workload": "%d requests drawn from %d seeded scans of the batched / served distribution%s" % (
-            len(pick), len(specs), "" if args.serve_full else " (rotations <= 8, slices <= 120)"),
-        "scans": desc,
-        "workers": args.serve_workers, "budget_gb": budget / 2**30,
-        "plain_scans_per_s": len(pick) / (plain_ms * 1e-3),
+        "workload": "%d requests, each one of %d seeded scans of the batched distribution or (5 %%, %d requests) "
+                    "a 40-turn 512^2 x 400-slice scan" % (n_req, args.serve_scans, pick.count(len(pool) - 1)),
+        "scans": desc, "per_scan_alone_ms": t_alone,
+        "workers": args.serve_workers, "budget_gb": budget / 2**30, "age_bound_ms": 2000.0,
+        "plain_scans_per_s": n_req / (plain_ms * 1e-3),
         "served_scans_per_s": served_rate,
-        "served_vs_plain": served_rate / (len(pick) / (plain_ms * 1e-3)),
+        "served_vs_plain": served_rate / (n_req / (plain_ms * 1e-3)),
         "served_voxel_updates_per_s": vu / (wall_sat * 1e-3),
         "poisson_rate_per_s": rate,
         "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99)},
         "plain_latency_ms_same_arrivals": {"p50": percentile(plain_lat, 0.5), "p99": percentile(plain_lat, 0.99)},
+        "requests_started_ahead_of_older": int(passed),
         "matches_alone": bool(same_sat and same_poi),
-        "entry_points": "ctbb_server_create / _submit / _wait (server) vs ctbb_reconstruct_scan_host (plain)",
+        "entry_points": "ctbb_server_create / _configure / _submit / _wait (server) vs ctbb_reconstruct_scan_host "
+                        "(plain)",
     }
 
 
