@@ -1333,14 +1333,17 @@ def serve_measure(args, torch):
 
 
 def run_profile_case(args):
-    """Block 0 of the config: its pull window generated on the device, then
-    adaptive filter, rebin, ramp filter and backprojection once each (about
-    2 GB on the device; every input is larger than L2)."""
+    """Block 0 of the configuration: its pull window generated on the device,
+    then adaptive filter, rebin, ramp filter (FP32 FFT) and backprojection
+    once each, then the reduced-storage stages on the same rebinned rows: the
+    tensor-core ramp filter into FP16 footprint words and the backprojection
+    from them.  A few GB on the device; every input is larger than L2."""
     import torch
 
     from ctbangbang_gb300 import lib as L
-    from ctbangbang_gb300 import scans, structs
+    from ctbangbang_gb300 import structs
     lib = L.load()
+    from ctbangbang_gb300 import scans
     spec = scans.CONFIGS[args.config]
     tmp = tempfile.TemporaryDirectory(prefix="ctbb_prof_")
     mr = make_plan(spec, tmp.name)
@@ -1352,31 +1355,53 @@ def run_profile_case(args):
     frame = m.cg.n_rows_raw * m.cg.n_channels
     P = b0.n_proj_pull
     nv = P // b0.n_ffs - 2 * m.cg.add_projections
+    nos, R = m.cg.n_channels_oversampled, m.cg.n_rows
     ta = torch.from_numpy(np.ctypeslib.as_array(mr.tube_angles, (n,)).copy()).cuda()
     tp = torch.from_numpy(np.ctypeslib.as_array(mr.table_positions, (n,)).copy()).cuda()
     d_raw = torch.empty(P * frame, dtype=torch.float32, device="cuda")
-    ctbb_synth.project_device(m, ctbb_synth.phantom_objects(spec), ta.data_ptr(), tp.data_ptr(), int(b0.idx_pull_start), P,
-                         spec.i0, spec.seed, d_raw.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    ctbb_synth.project_device(m, ctbb_synth.phantom_objects(spec), ta.data_ptr(), tp.data_ptr(), int(b0.idx_pull_start),
+                              P, spec.i0, spec.seed, d_raw.data_ptr(), torch.cuda.current_stream().cuda_stream)
     d_filt = torch.empty_like(d_raw)
-    d_rb = torch.empty(nv * m.cg.n_rows * m.cg.n_channels_oversampled, dtype=torch.float32, device="cuda")
+    d_rb = torch.empty(nv * R * nos, dtype=torch.float32, device="cuda")
     d_blk = torch.empty(m.rp.nx * m.rp.ny * m.ri.n_slices_block, dtype=torch.float32, device="cuda")
-    taps = (C.c_float * (2 * m.cg.n_channels_oversampled))()
+    taps = (C.c_float * (2 * nos))()
     L.call("ctbb_load_filter", C.byref(m), taps)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(12)]
     ev[0].record()
     L.call("ctbb_adaptive_filter_device", C.byref(m), C.c_void_p(d_raw.data_ptr()), C.c_void_p(d_filt.data_ptr()))
     ev[1].record()
-    L.call("ctbb_rebin_device", C.byref(m), C.c_void_p(d_filt.data_ptr()), C.c_void_p(d_rb.data_ptr()))
     ev[2].record()
-    L.call("ctbb_ramp_filter_device", C.c_void_p(d_rb.data_ptr()), nv * m.cg.n_rows, m.cg.n_channels_oversampled, taps)
+    L.call("ctbb_rebin_device", C.byref(m), C.c_void_p(d_filt.data_ptr()), C.c_void_p(d_rb.data_ptr()))
     ev[3].record()
-    L.call("ctbb_backproject_device", C.byref(m), C.c_void_p(d_rb.data_ptr()), C.c_void_p(d_blk.data_ptr()))
+    del d_raw, d_filt
+    d_unfilt = d_rb.clone()
     ev[4].record()
+    L.call("ctbb_ramp_filter_device", C.c_void_p(d_rb.data_ptr()), nv * R, nos, taps)
+    ev[5].record()
+    ev[6].record()
+    L.call("ctbb_backproject_device", C.byref(m), C.c_void_p(d_rb.data_ptr()), C.c_void_p(d_blk.data_ptr()))
+    ev[7].record()
+    del d_rb
+    quads = torch.empty(nv * R * nos * 4, dtype=torch.float16, device="cuda")
+    qscale = torch.empty(nv * R, dtype=torch.float32, device="cuda")
+    ev[8].record()
+    L.call("ctbb_ramp_filter_fp16_device", C.c_void_p(d_unfilt.data_ptr()), nv * R, nos, taps, R,
+           C.c_void_p(quads.data_ptr()), C.c_void_p(qscale.data_ptr()))
+    ev[9].record()
+    d_blk16 = torch.empty_like(d_blk)
+    ev[10].record()
+    L.call("ctbb_backproject_fp16_device", C.byref(m), C.c_void_p(quads.data_ptr()), C.c_void_p(qscale.data_ptr()),
+           C.c_void_p(d_blk16.data_ptr()))
+    ev[11].record()
     torch.cuda.synchronize()
-    ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    ms = [ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(6)]
+    from ctbangbang_gb300.scans import MU_WATER
+    diff = (d_blk16 - d_blk).double().abs() * (1000.0 / MU_WATER)
     print(json.dumps({"profile_case": args.config, "block": 0, "n_proj_pull": P, "n_views": nv,
-                      "stage_ms": dict(zip(STAGES[:4], ms)),
-                      "finite": bool(torch.isfinite(d_blk).all().item())}), flush=True)
+                      "stage_ms": dict(zip(STAGES[:4] + ["ramp_filter_fp16_tensor", "backproject_fp16"], ms)),
+                      "fp16_vs_fp32_block_hu": {"max": float(diff.max()), "rms": float(diff.pow(2).mean().sqrt())},
+                      "finite": bool(torch.isfinite(d_blk).all().item() and torch.isfinite(d_blk16).all().item())}),
+          flush=True)
     scans.free_plan(mr)
 
 

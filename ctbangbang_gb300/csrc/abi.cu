@@ -572,6 +572,28 @@ extern "C" int ctbb_ramp_filter_fp16_device(const float *d_lines, size_t n_lines
     return ramp_tc_check(c.ramp_tc, c.stream);
 }
 
+extern "C" int ctbb_backproject_fp16_device(const struct recon_metadata *mr, const void *d_quads,
+                                            const float *d_scale, float *d_block)
+{
+    clear_error();
+    CTBB_TRY(check_mr(mr));
+    if (!d_quads || !d_scale || !d_block) {
+        set_error("ctbb_backproject_fp16_device: null buffer");
+        return CTBB_ERR_ARGUMENT;
+    }
+    Context &c = ctx();
+    CTBB_TRY(require_device(c));
+    std::lock_guard<std::mutex> lk(c.mu);
+    BackprojectTables t;
+    CTBB_TRY(build_backproject_tables(*mr, &t));
+    CTBB_TRY(upload(c.bp_views, t.views, c.stream));
+    CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
+    CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    StageScope scope(c, 3);
+    return launch_backproject(*mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
+                              static_cast<const float *>(d_quads), d_block, 8, c.stream, d_scale);
+}
+
 extern "C" int ctbb_backproject_device(const struct recon_metadata *mr, const float *d_rebin, float *d_block)
 {
     clear_error();

@@ -57,6 +57,7 @@ PROTOTYPES = {
     "ctbb_autotune_report": (C.c_int, [C.c_char_p, C.c_size_t]),
     "ctbb_context_set_storage": (C.c_int, [C.c_void_p, C.c_int]),
     "ctbb_backproject_device": (C.c_int, [_MR, _VP, _VP]),
+    "ctbb_backproject_fp16_device": (C.c_int, [_MR, _VP, _VP, _VP]),
     "ctbb_scan_workspace_bytes": (C.c_size_t, [_MR]),
     "ctbb_server_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]),
     "ctbb_server_submit": (C.c_int, [C.c_void_p, _MR, _F, _F, C.c_float, C.POINTER(C.c_uint64)]),

@@ -356,6 +356,13 @@ int ctbb_ramp_filter_fp16_device(const float *d_lines, size_t n_lines, int n_os,
 int ctbb_backproject_device(const struct recon_metadata *mr,
                             const float *d_rebin, float *d_block);
 
+/* ctbb_backproject_device from the reduced-storage rows: d_quads, the FP16
+   footprint words of one block's views as ctbb_ramp_filter_fp16_device
+   writes them with rows_per_view = n_rows ([n_views][n_rows][n_os][4]), and
+   d_scale [n_views * n_rows] their scales (one per view); FP32 accumulation. */
+int ctbb_backproject_fp16_device(const struct recon_metadata *mr, const void *d_quads, const float *d_scale,
+                                 float *d_block);
+
 /* Reorder + thicken d_image [n_slices_recon][ny][nx] into
    d_final [n_slices_final][ny][nx]; mu_water > 0 also converts to HU. */
 int ctbb_finalize_device(const struct recon_metadata *mr, const float *d_image,
