@@ -816,7 +816,7 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
 
 def measure_fp16(args, torch, lib, m, ref):
     """The reduced-storage mode on the headline scan: the ramp filter as the
-    BF16 hi/lo Toeplitz contraction on the tensor cores writing FP16 footprint
+    FP16 hi/lo Toeplitz contraction on the tensor cores writing FP16 footprint
     rows with per-view scales, the backprojector reading them (FP32
     accumulation).  Device-resident steps, stage profile, tensor-pipe
     throughput of the filter, HU errors of the output against the FP64 oracle
@@ -852,7 +852,7 @@ def measure_fp16(args, torch, lib, m, ref):
     ms = e0.elapsed_time(e1) / args.steps
     diff = (d_out - d_ref).double().abs()
     hu = 1000.0 / scans.MU_WATER
-    # the filter's tensor work: 3 BF16 products of 2 n^2 FLOP per row over the
+    # the filter's tensor work: 3 FP16 products of 2 n^2 FLOP per row over the
     # union's rows and the edge views' rows
     n = mr.cg.n_channels_oversampled
     filter_rows = (sizes["union_rebin_samples"] // n)

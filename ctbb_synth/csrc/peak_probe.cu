@@ -1,8 +1,8 @@
 // peak_probe.cu -- FP32 FMA throughput of the device, measured.
 //
 // The backprojector is bound by the FP32 pipe; its roofline needs the FP32
-// peak of this GPU under the clocks of the run (the measured peaks of the
-// pool hold HBM and BF16 figures only).  Measurement infrastructure, built
+// peak of this GPU under the clocks of the run (the measured peak figures
+// at hand are HBM and BF16 only).  Measurement infrastructure, built
 // into libctbb_synth.so, not into the reconstruction library.  Each thread runs 16
 // independent FMA chains (enough to hide the FMA latency) for a fixed number
 // of iterations on registers only; the result is stored so the work is kept.

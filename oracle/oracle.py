@@ -5,8 +5,8 @@
                   `make -C oracle` on first use; plain g++).
   reference()  -> ctypes handle of oracle/_ref/libctbb_ref.so, the reference's
                   own CPU sources compiled with oracle/ref/Makefile, or None when
-                  the reference tree is not available (the GPU machine) and nothing
-                  was built.
+                  the reference tree is not available on this machine and
+                  nothing was built.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and reference
 arm import this module.  The product never does.
