@@ -725,6 +725,8 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
+        lib.ctbb_profile_read(None, None, 0, 1)
+        lib.ctbb_profile_enable(1)
         t0 = time.perf_counter()
         c0 = time.thread_time()
         for _ in range(args.steps):
@@ -732,6 +734,10 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
         torch.cuda.synchronize()
         e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
         cpu_ms = (time.thread_time() - c0) * 1e3 / args.steps
+        lib.ctbb_profile_enable(0)
+        e_stage_ms = (C.c_double * 5)()
+        lib.ctbb_profile_read(e_stage_ms, None, 5, 1)
+        e_stages = {name: e_stage_ms[i] / args.steps for i, name in enumerate(STAGES)}
         same = bool(torch.equal(h_final.cuda(), d_final))
         h2d_ms, d2h_ms = time_h2d_d2h(torch, h_scan, out["h2d_bytes"], n_final * plane * 4)
         out["e2e"] = {
@@ -743,9 +749,12 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
                 "h2d_copy_alone": h2d_ms, "d2h_copy_alone": d2h_ms,
                 "h2d_gbs": out["h2d_bytes"] / (h2d_ms * 1e-3) / 1e9,
                 "calling_thread_cpu": cpu_ms,
+                "stages_ms_per_step": e_stages,
+                "compute_stream_idle": e_ms - sum(e_stages.values()),
                 "note": "the host path streams the copy in chunks under the compute: e2e = device step + the "
-                        "first chunk's copy + what does not overlap; calling_thread_cpu includes the wait "
-                        "for the stream (a spinning synchronise)"}}
+                        "first chunk's copy + what does not overlap; stages_ms_per_step are the compute "
+                        "stream's stage times in the e2e steps and compute_stream_idle the rest of the step; "
+                        "calling_thread_cpu includes the wait for the stream (a spinning synchronise)"}}
         if headline and not args.no_whole_scan:
             def ws_host_step():
                 L.call(alt_host, C.byref(mr), hp, fp, C.c_float(0.0))

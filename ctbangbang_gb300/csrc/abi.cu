@@ -76,8 +76,9 @@ struct Context {
     DeviceBuffer raw_in, raw_filt, rebin, block, image, final_stack, scratch;
     // tables
     DeviceBuffer bp_views, bp_theta, bp_zpos, fin_offsets, fin_slices, fin_weights;
-    // whole-scan paths: one block window filtered with its own statistics
-    DeviceBuffer edge_raw;
+    // whole-scan paths: one block window filtered with its own statistics,
+    // and per frame of each block window whether that can differ from the union
+    DeviceBuffer edge_raw, dirty;
     DeviceRebinTables rebin_tables;
     RampFilterPlan ramp;
     RampTcPlan ramp_tc;
@@ -293,17 +294,16 @@ static int do_filter(Context &c, const struct recon_metadata &mr, float *d_rebin
 }
 
 // Where the rows of a block's views sit in the whole-scan paths' rows buffer:
-// view j (= i + k n_half) is row off + j of the union's rows, except views
-// [0, d0) and [d1, n_used), which were re-made from the block's own window
-// (EdgePlan) into rows patch, patch + 1, ... in that order.
+// view j (= i + k n_half) is row off + j of the union's rows, except the
+// views re-made from the block's own window (EdgePlan, dirty_view_runs),
+// which sit at row patch + slot[j].
 struct ViewRows {
     size_t off = 0;
-    int d0 = 0, d1 = 0, n_used = 0;
     size_t patch = 0;
+    std::vector<int> slot;  // per view: -1, or its row in the patch rows
     unsigned row(int j) const
     {
-        if (j < d0) return (unsigned)(patch + j);
-        if (j >= d1) return (unsigned)(patch + d0 + (j - d1));
+        if (j < (int)slot.size() && slot[(size_t)j] >= 0) return (unsigned)(patch + (size_t)slot[(size_t)j]);
         return (unsigned)(off + j);
     }
 };
@@ -443,7 +443,7 @@ static void release_context(Context &c, bool device_sync, bool unbind)
     }
     for (DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                             &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                            &c.fin_weights, &c.edge_raw})
+                            &c.fin_weights, &c.edge_raw, &c.dirty})
         b->release();
     if (c.rebin_tables.base) cudaFree(c.rebin_tables.base);
     c.rebin_tables = DeviceRebinTables{};
@@ -788,13 +788,16 @@ static EdgePlan edge_plan(const struct recon_metadata &mb, long long g0, long lo
     return e;
 }
 
-// Largest pull window and edge patch (views) over the blocks of a plan.
+// Largest pull window and edge patch (views) over the blocks of a plan; the
+// sums of the edge patches and of the pull windows of blocks with edge views.
 static void edge_extent(const struct recon_metadata &mr, const std::vector<struct recon_info> &blocks,
-                        long long g0, long long g1, size_t *max_pull, size_t *max_patch, size_t *sum_patch = nullptr)
+                        long long g0, long long g1, size_t *max_pull, size_t *max_patch, size_t *sum_patch = nullptr,
+                        size_t *sum_edge_pull = nullptr)
 {
     *max_pull = 0;
     *max_patch = 0;
     if (sum_patch) *sum_patch = 0;
+    if (sum_edge_pull) *sum_edge_pull = 0;
     for (const auto &ri : blocks) {
         struct recon_metadata mb = mr;
         mb.ri = ri;
@@ -802,41 +805,115 @@ static void edge_extent(const struct recon_metadata &mr, const std::vector<struc
         *max_pull = std::max(*max_pull, (size_t)ri.n_proj_pull);
         *max_patch = std::max(*max_patch, (size_t)e.n_patch());
         if (sum_patch) *sum_patch += (size_t)e.n_patch();
+        if (sum_edge_pull && e.any()) *sum_edge_pull += (size_t)ri.n_proj_pull;
     }
 }
 
-// Re-makes the edge views of block mb: its window's thresholds from its own
+// First step of a block's edge views: its window's thresholds from its own
 // statistics (the frames' maxima are the union's, d_union_sup at the block's
-// offset), frames [0, fa) and [fb, P) of the window filtered into c.edge_raw,
-// the block's views [0, d0) and [d1, n_used) rebinned from there with the
-// block's own view-axis coordinates (the tables are the union's; only the
-// window length differs) into d_patch, and ramp-filtered.
-static int run_edge_patch(Context &c, const struct recon_metadata &mb, const EdgePlan &e, const RebinTables &rt,
-                          const float *d_union_raw, const float *d_union_sup, long long g0, float *d_block_scratch,
-                          size_t patch_view)
+// offset; d_block_scratch holds 6 P floats), and per frame of the window
+// whether its filtered value can differ from the union's (d_dirty, P bytes),
+// given the union's thresholds d_union_thr.
+static int edge_dirty_frames(Context &c, const struct recon_metadata &mb, const EdgePlan &e,
+                             const float *d_union_raw, const float *d_union_sup, const float *d_union_thr,
+                             long long g0, long long g1, float *d_block_scratch, unsigned char *d_dirty)
 {
     BlockDims d = block_dims(mb);
-    float *d_patch = c.rebin.as<float>() + patch_view * d.n_rows * d.n_os;
+    const size_t frame = d.n_rows_raw * d.n_channels;
+    const long long sb = (long long)(int)mb.ri.idx_pull_start - g0;
+    const int lo_edge = sb > 0 ? 1 : 0;
+    const int hi_edge = (long long)(int)mb.ri.idx_pull_start + (long long)d.n_proj_pull < g1 ? 1 : 0;
+    StageScope scope(c, 0);
+    CTBB_TRY(launch_adaptive_filter_ends_thresholds(mb, d_union_raw + (size_t)sb * frame, d_union_sup + sb,
+                                                    d_block_scratch, e.fa, e.fb, c.stream));
+    return launch_adaptive_filter_dirty(mb, d_union_sup + sb, d_union_thr + sb, d_block_scratch, e.fa, e.fb,
+                                        lo_edge, hi_edge, d_dirty, c.stream);
+}
+
+// The block's rebin tables: the union's with the block's own window length
+// and float view-axis coordinates, as its block loop.
+static RebinTables block_rebin_tables(const RebinTables &rt, const BlockDims &d)
+{
+    RebinTables tb = rt;
+    tb.split_view_coord = 0;
+    tb.n_proj = (int)(d.n_proj_pull / d.n_ffs);
+    tb.n_views = tb.n_proj - 2 * tb.add_projections;
+    return tb;
+}
+
+// Runs [j0, j1) of the block's edge views that read a frame whose filtered
+// value can differ from the union's (dirty, one byte per frame of the
+// block's window): view j reads frames [n_ffs (j - 2), rebin_frames_needed(j)).
+// Runs closer than kRunGap views are joined (fewer launches; a joined view
+// re-made from the block's window is as exact as the union's).
+static std::vector<std::pair<int, int>> dirty_view_runs(const EdgePlan &e, const RebinTables &tb,
+                                                        const unsigned char *dirty, int P)
+{
+    constexpr int kRunGap = 32;
+    std::vector<int> cum((size_t)P + 1, 0);
+    for (int f = 0; f < P; ++f) cum[(size_t)f + 1] = cum[(size_t)f] + (dirty[f] ? 1 : 0);
+    std::vector<std::pair<int, int>> runs;
+    if (cum[(size_t)P] == 0) return runs;
+    auto scan = [&](int v0, int v1) {
+        int run0 = -1, last = -1;
+        for (int j = v0; j < v1; ++j) {
+            const int a = std::max(0, tb.n_ffs * (j - 2));
+            const int b = std::min(P, rebin_frames_needed(tb, j));
+            if (b <= a || cum[(size_t)b] == cum[(size_t)a]) continue;
+            if (run0 >= 0 && j - last <= kRunGap) {
+                last = j;
+                continue;
+            }
+            if (run0 >= 0) runs.emplace_back(run0, last + 1);
+            run0 = last = j;
+        }
+        if (run0 >= 0) runs.emplace_back(run0, last + 1);
+    };
+    scan(0, e.d0);
+    scan(e.d1, e.n_used);
+    return runs;
+}
+
+// Re-makes the runs of block mb's edge views: their frames of the block's
+// window filtered with the block's own thresholds (left in d_block_scratch
+// by edge_dirty_frames) into c.edge_raw, the views rebinned from there into
+// the rows from patch_view on, in run order, and ramp-filtered; vr->slot
+// records where each landed and *n_made counts the views.
+static int run_edge_patch(Context &c, const struct recon_metadata &mb, const RebinTables &rt,
+                          const std::vector<std::pair<int, int>> &runs, const float *d_union_raw,
+                          const float *d_union_sup, long long g0, float *d_block_scratch, size_t patch_view,
+                          ViewRows *vr, size_t *n_made)
+{
+    *n_made = 0;
+    if (runs.empty()) return CTBB_OK;
+    BlockDims d = block_dims(mb);
     const size_t frame = d.n_rows_raw * d.n_channels;
     const size_t view_elems = d.n_rows * d.n_os;
     const long long sb = (long long)(int)mb.ri.idx_pull_start - g0;
-    {
-        StageScope scope(c, 0);
-        CTBB_TRY(launch_adaptive_filter_ends(mb, d_union_raw + (size_t)sb * frame, c.edge_raw.as<float>(),
-                                             d_union_sup + sb, d_block_scratch, e.fa, e.fb, c.stream));
+    const int P = (int)d.n_proj_pull;
+    const RebinTables tb = block_rebin_tables(rt, d);
+    size_t slot = 0;
+    for (const auto &r : runs) {
+        const int f0 = std::max(0, tb.n_ffs * (r.first - 2));
+        const int f1 = std::min(P, rebin_frames_needed(tb, r.second - 1));
+        {
+            StageScope scope(c, 0);
+            CTBB_TRY(launch_adaptive_filter_output(mb, d_union_raw + (size_t)sb * frame, c.edge_raw.as<float>(),
+                                                   d_union_sup + sb, d_block_scratch, f0, f1, c.stream));
+        }
+        // view v of the run lands in row patch_view + slot + (v - r.first)
+        float *d_out = c.rebin.as<float>() + (patch_view + slot) * view_elems - (size_t)r.first * view_elems;
+        {
+            StageScope scope(c, 1);
+            CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(), d_out, c.stream, r.first, r.second));
+        }
+        const size_t n = (size_t)(r.second - r.first);
+        CTBB_TRY(filter_scan_rows(c, (patch_view + slot) * d.n_rows, n * d.n_rows, (int)d.n_rows, (int)d.n_os));
+        for (int j = r.first; j < r.second; ++j) vr->slot[(size_t)j] = (int)(slot + (size_t)(j - r.first));
+        slot += n;
     }
-    RebinTables tb = rt;
-    tb.split_view_coord = 0;  // the block's own float coordinates, as its block loop
-    tb.n_proj = (int)(d.n_proj_pull / d.n_ffs);
-    tb.n_views = tb.n_proj - 2 * tb.add_projections;
-    {
-        StageScope scope(c, 1);
-        if (e.d0 > 0) CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(), d_patch, c.stream, 0, e.d0));
-        if (e.d1 < e.n_used)
-            CTBB_TRY(launch_rebin(tb, c.rebin_tables, c.edge_raw.as<float>(),
-                                  d_patch - (size_t)(e.d1 - e.d0) * view_elems, c.stream, e.d1, e.n_used));
-    }
-    return filter_scan_rows(c, patch_view * d.n_rows, (size_t)e.n_patch() * d.n_rows, (int)d.n_rows, (int)d.n_os);
+    *n_made = slot;
+    return CTBB_OK;
 }
 
 // Device bytes the whole-scan paths (scan_device / scan_host / scan_file)
@@ -854,13 +931,14 @@ extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
     BlockDims dg = block_dims(mg);
     const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
     const int n_final = ctbb_n_slices_final(mr);
-    size_t max_pull = 0, max_patch = 0, sum_patch = 0;
-    edge_extent(m, blocks, g0, g1, &max_pull, &max_patch, &sum_patch);
+    size_t max_pull = 0, max_patch = 0, sum_patch = 0, sum_edge_pull = 0;
+    edge_extent(m, blocks, g0, g1, &max_pull, &max_patch, &sum_patch, &sum_edge_pull);
     const size_t frame = dg.n_rows_raw * dg.n_channels, view_elems = dg.n_rows * dg.n_os;
     return (2 * dg.raw_elems() + dg.rebin_elems() + sum_patch * view_elems + max_pull * frame +
-            adaptive_filter_scratch_floats(dg.n_proj_pull) + adaptive_filter_scratch_floats(max_pull) +
-            plane * mr->ri.n_slices_recon + plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
-           ((size_t)8 << 20);
+            adaptive_filter_scratch_floats(dg.n_proj_pull) +
+            adaptive_filter_scratch_floats(std::max(max_pull, sum_edge_pull)) + plane * mr->ri.n_slices_recon +
+            plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
+           sum_edge_pull + ((size_t)8 << 20);
 }
 
 
@@ -913,8 +991,25 @@ static int prepare_scan_device(Context &c, struct recon_metadata *mr, const floa
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
     size_t max_pull = 0, max_patch = 0, sum_patch = 0;
     edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch, &sum_patch);
+    // scratch: the union's statistics, then each block's (6 P floats each);
+    // dirty: one byte per frame of each block's window
     const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
-    CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
+    std::vector<EdgePlan> plans(blocks.size());
+    std::vector<size_t> af_off(blocks.size(), 0), dirty_off(blocks.size(), 0);
+    size_t af_total = af_union, dirty_total = 0;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        mr->ri = blocks[b];
+        plans[b] = edge_plan(*mr, g0, g1);
+        if (!plans[b].any()) continue;
+        af_off[b] = af_total;
+        dirty_off[b] = dirty_total;
+        af_total += adaptive_filter_scratch_floats(blocks[b].n_proj_pull);
+        dirty_total += blocks[b].n_proj_pull;
+    }
+    CTBB_TRY(c.scratch.ensure(af_total * sizeof(float)));
+    if (dirty_total) CTBB_TRY(c.dirty.ensure(dirty_total));
+    float *d_union_sup = c.scratch.as<float>();
+    const float *d_union_thr = c.scratch.as<float>() + 5 * (size_t)dg.n_proj_pull;  // af_params' thr slot
     {
         StageScope scope(c, 0);
         CTBB_TRY(launch_adaptive_filter(mg, d_win, c.raw_filt.as<float>(), c.scratch.as<float>(), c.stream));
@@ -928,9 +1023,23 @@ static int prepare_scan_device(Context &c, struct recon_metadata *mr, const floa
         StageScope scope(c, 1);
         CTBB_TRY(launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream));
     }
+    // each block's edge frames that can filter differently from the union
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        if (!plans[b].any()) continue;
+        mr->ri = blocks[b];
+        CTBB_TRY(edge_dirty_frames(c, *mr, plans[b], d_win, d_union_sup, d_union_thr, g0, g1,
+                                   c.scratch.as<float>() + af_off[b], c.dirty.as<unsigned char>() + dirty_off[b]));
+    }
     CTBB_TRY(filter_scan_rows(c, 0, dg.n_views * dg.n_rows, (int)dg.n_rows, (int)dg.n_os));
+    // the flags come back once the union is filtered (the copy waits for the
+    // stream; the device has the union's rows to make meanwhile)
+    std::vector<unsigned char> dirty(dirty_total);
+    if (dirty_total) {
+        CTBB_CUDA_TRY(cudaMemcpyAsync(dirty.data(), c.dirty.ptr, dirty_total, cudaMemcpyDeviceToHost, c.stream));
+        CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
     if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
-    // every block's edge views in rows of their own, and its tables
+    // the re-made edge views of every block in rows of their own, and its tables
     prep->rows.assign(blocks.size(), ViewRows{});
     prep->tables.assign(blocks.size(), BackprojectTables{});
     prep->table_off.assign(blocks.size(), 0);
@@ -940,15 +1049,18 @@ static int prepare_scan_device(Context &c, struct recon_metadata *mr, const floa
         mr->ri = blocks[b];
         ViewRows &vr = prep->rows[b];
         vr.off = union_view_offset(blocks[b], g0);
-        EdgePlan e = edge_plan(*mr, g0, g1);
-        vr.d0 = e.d0;
-        vr.d1 = e.d1;
-        vr.n_used = e.n_used;
         vr.patch = patch_view;
-        if (e.any())
-            CTBB_TRY(run_edge_patch(c, *mr, e, rt, d_win, c.scratch.as<float>(), g0, c.scratch.as<float>() + af_union,
-                                    patch_view));
-        patch_view += (size_t)e.n_patch();
+        const EdgePlan &e = plans[b];
+        if (e.any()) {
+            BlockDims db = block_dims(*mr);
+            const auto runs = dirty_view_runs(e, block_rebin_tables(rt, db), dirty.data() + dirty_off[b],
+                                              (int)db.n_proj_pull);
+            vr.slot.assign((size_t)e.n_used, -1);
+            size_t made = 0;
+            CTBB_TRY(run_edge_patch(c, *mr, rt, runs, d_win, d_union_sup, g0, c.scratch.as<float>() + af_off[b],
+                                    patch_view, &vr, &made));
+            patch_view += made;
+        }
         BackprojectTables &t = prep->tables[b];
         CTBB_TRY(build_backproject_tables(*mr, &t));
         for (int i = 0; i < t.n_half; ++i)
@@ -1502,7 +1614,10 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
     CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
     CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
-    if (max_patch) CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
+    if (max_patch) {
+        CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
+        CTBB_TRY(c.dirty.ensure(max_pull));
+    }
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
     CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
     // the union window in chunks of whole focal-spot cycles; the copy stream
@@ -1572,17 +1687,32 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             if (need > (size_t)v_done && v_done < V) break;
             EdgePlan e = edge_plan(mb, g0, g1);
             const long long sb = (long long)(int)blocks[b_done].idx_pull_start - g0;
-            if (e.any() && af.n_sup < sb + (long long)db.n_proj_pull) break;
+            // edge views: the union's thresholds of the block's whole window
+            if (e.any() && af.filtered() < std::min((long long)G, sb + (long long)db.n_proj_pull)) break;
             mr->ri = blocks[b_done];
             ViewRows vr;
             vr.off = union_view_offset(blocks[b_done], g0);
-            vr.d0 = e.d0;
-            vr.d1 = e.d1;
-            vr.n_used = e.n_used;
             vr.patch = dg.n_views;
-            if (e.any())
-                status = run_edge_patch(c, mb, e, rt, d_raw, c.scratch.as<float>(), g0,
-                                        c.scratch.as<float>() + af_union, dg.n_views);
+            if (e.any()) {
+                float *d_block_scratch = c.scratch.as<float>() + af_union;
+                status = edge_dirty_frames(c, mb, e, d_raw, c.scratch.as<float>(),
+                                           c.scratch.as<float>() + 5 * (size_t)dg.n_proj_pull, g0, g1,
+                                           d_block_scratch, c.dirty.as<unsigned char>());
+                std::vector<unsigned char> dirty(db.n_proj_pull);
+                if (status == CTBB_OK &&
+                    (cudaMemcpyAsync(dirty.data(), c.dirty.ptr, dirty.size(), cudaMemcpyDeviceToHost, c.stream) !=
+                         cudaSuccess ||
+                     cudaStreamSynchronize(c.stream) != cudaSuccess)) {
+                    set_error("whole scan: reading the edge frames' flags failed");
+                    status = CTBB_ERR_CUDA;
+                }
+                if (status != CTBB_OK) break;
+                const auto runs = dirty_view_runs(e, block_rebin_tables(rt, db), dirty.data(), (int)db.n_proj_pull);
+                vr.slot.assign((size_t)e.n_used, -1);
+                size_t made = 0;
+                status = run_edge_patch(c, mb, rt, runs, d_raw, c.scratch.as<float>(), g0, d_block_scratch,
+                                        dg.n_views, &vr, &made);
+            }
             if (status != CTBB_OK) break;
             float *slab = c.image.as<float>() + b_done * n_block * plane;
             status = backproject_scan_rows(c, *mr, slab, vr);
@@ -1921,7 +2051,8 @@ static size_t context_device_bytes(const Context &c)
     size_t n = 0;
     for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                                   &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                                  &c.fin_weights, &c.edge_raw, &c.tc_work, &c.quads, &c.qscale, &c.bp_tables})
+                                  &c.fin_weights, &c.edge_raw, &c.dirty, &c.tc_work, &c.quads, &c.qscale,
+                                  &c.bp_tables})
         n += b->bytes;
     return n + c.ramp.capacity * sizeof(float2);
 }

@@ -318,6 +318,27 @@ __global__ void __launch_bounds__(256) af_filter_stream_kernel(AfParams p)
     }
 }
 
+// One thread per frame of the window: can this window's filtered frame
+// differ from the larger window's?  Not when no sample exceeds either
+// threshold (every sample is at most the frame's maximum sup), and not when
+// the thresholds agree and the smoothing stencil does not reach past this
+// window's ends where the larger window goes on.  NaN thresholds count as
+// differing.
+__global__ void af_dirty_kernel(const float *sup, const float *thr_union, const float *thr, int P, int fa, int fb,
+                                int lo_edge, int hi_edge, unsigned char *dirty)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= P) return;
+    unsigned char d = 0;
+    if (f < fa || f >= fb) {
+        const float s = sup[f], tb = thr[f], tu = thr_union[f];
+        const bool end = (lo_edge && f < 2) || (hi_edge && f >= P - 2);
+        const bool same = (s <= tb && s <= tu) || (tb == tu && !end);
+        d = same ? 0 : 1;
+    }
+    dirty[f] = d;
+}
+
 }  // namespace
 
 size_t adaptive_filter_scratch_floats(size_t n_proj_pull) { return 6 * n_proj_pull; }
@@ -359,10 +380,13 @@ int af_params(const struct recon_metadata &mr, const float *d_in, float *d_out, 
 }
 
 // The five steps over frame ranges: maxima of [sup0, sup1), moving means of
-// [smooth0, smooth1), eccentricity, threshold and smoothing of [out0, out1).
-// Each range may be empty; a step reads the earlier steps' results of the
-// frames its windows cover, which the caller has launched before.
-int af_launch(AfParams p, int sup0, int sup1, int smooth0, int smooth1, int out0, int out1, cudaStream_t stream)
+// [smooth0, smooth1), eccentricity, threshold and smoothing of [out0, out1)
+// (eccentricity and threshold only with `thresholds`, smoothing only with
+// `output`).  Each range may be empty; a step reads the earlier steps'
+// results of the frames its windows cover, which the caller has launched
+// before.
+int af_launch(AfParams p, int sup0, int sup1, int smooth0, int smooth1, int out0, int out1, cudaStream_t stream,
+              bool thresholds = true, bool output = true)
 {
     int launches = 0;
     if (sup1 > sup0) {
@@ -377,12 +401,18 @@ int af_launch(AfParams p, int sup0, int sup1, int smooth0, int smooth1, int out0
         af_smooth_kernel<<<(smooth1 - smooth0 + 127) / 128, 128, 0, stream>>>(p);
         ++launches;
     }
-    if (out1 > out0) {
+    if (out1 > out0 && thresholds) {
         int n = out1 - out0;
         p.f0 = out0;
         p.f1 = out1;
         af_ecc_kernel<<<(n + 127) / 128, 128, 0, stream>>>(p);
         af_threshold_kernel<<<(n * 32 + 255) / 256, 256, 0, stream>>>(p);
+        launches += 2;
+    }
+    if (out1 > out0 && output) {
+        int n = out1 - out0;
+        p.f0 = out0;
+        p.f1 = out1;
         if (p.N % 4 == 0) {
             af_filter_stream_kernel<<<n, 256, 0, stream>>>(p);
         } else {
@@ -393,7 +423,7 @@ int af_launch(AfParams p, int sup0, int sup1, int smooth0, int smooth1, int out0
             }
             af_filter_kernel<<<grid, 256, 0, stream>>>(p);
         }
-        launches += 3;
+        launches += 1;
     }
     count_launch(launches);
     CTBB_CUDA_TRY(cudaGetLastError());
@@ -418,16 +448,43 @@ int adaptive_filter_edge_reach(const struct recon_metadata &mr)
     return p.range_offset + p.avg_offset;
 }
 
-int launch_adaptive_filter_ends(const struct recon_metadata &mr, const float *d_in, float *d_out,
-                                const float *d_sup, float *d_scratch, int fa, int fb, cudaStream_t stream)
+int launch_adaptive_filter_ends_thresholds(const struct recon_metadata &mr, const float *d_in, const float *d_sup,
+                                           float *d_scratch, int fa, int fb, cudaStream_t stream)
 {
     AfParams p;
-    CTBB_TRY(af_params(mr, d_in, d_out, d_scratch, &p));
+    CTBB_TRY(af_params(mr, d_in, nullptr, d_scratch, &p));
     p.sup = const_cast<float *>(d_sup);  // read only: no maxima are launched
     fa = std::min(std::max(fa, 0), p.P);
     fb = std::min(std::max(fb, fa), p.P);
-    CTBB_TRY(af_launch(p, 0, 0, 0, p.P, 0, fa, stream));
-    return af_launch(p, 0, 0, 0, 0, fb, p.P, stream);
+    CTBB_TRY(af_launch(p, 0, 0, 0, p.P, 0, fa, stream, true, false));
+    return af_launch(p, 0, 0, 0, 0, fb, p.P, stream, true, false);
+}
+
+int launch_adaptive_filter_dirty(const struct recon_metadata &mr, const float *d_sup, const float *d_thr_union,
+                                 const float *d_scratch, int fa, int fb, int lo_edge, int hi_edge,
+                                 unsigned char *d_dirty, cudaStream_t stream)
+{
+    AfParams p;
+    float dummy = 0.0f;
+    CTBB_TRY(af_params(mr, &dummy, &dummy, const_cast<float *>(d_scratch), &p));
+    fa = std::min(std::max(fa, 0), p.P);
+    fb = std::min(std::max(fb, fa), p.P);
+    af_dirty_kernel<<<(p.P + 255) / 256, 256, 0, stream>>>(d_sup, d_thr_union, p.thr, p.P, fa, fb, lo_edge,
+                                                              hi_edge, d_dirty);
+    count_launch(1);
+    CTBB_CUDA_TRY(cudaGetLastError());
+    return CTBB_OK;
+}
+
+int launch_adaptive_filter_output(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                                  const float *d_sup, float *d_scratch, int f0, int f1, cudaStream_t stream)
+{
+    AfParams p;
+    CTBB_TRY(af_params(mr, d_in, d_out, d_scratch, &p));
+    p.sup = const_cast<float *>(d_sup);
+    f0 = std::min(std::max(f0, 0), p.P);
+    f1 = std::min(std::max(f1, f0), p.P);
+    return af_launch(p, 0, 0, 0, 0, f0, f1, stream, false, true);
 }
 
 AfStream::AfStream(const struct recon_metadata &mr) : P((int)mr.ri.n_proj_pull)

@@ -24,11 +24,28 @@ int adaptive_filter_edge_reach(const struct recon_metadata &mr);
 
 // The filter of one pull window whose per-frame maxima are given (d_sup, P
 // floats: the maxima of a larger window at this window's offset -- a frame's
-// maximum does not depend on the window): moving means of every frame, then
-// thresholds and output of frames [0, fa) and [fb, P) only.  d_scratch holds
-// 6 * P floats (the sup slot is not used).
-int launch_adaptive_filter_ends(const struct recon_metadata &mr, const float *d_in, float *d_out,
-                                const float *d_sup, float *d_scratch, int fa, int fb, cudaStream_t stream);
+// maximum does not depend on the window), in three steps for a caller that
+// decides between them which frames it needs.  d_scratch holds 6 * P floats
+// (its sup slot is not used).
+//  * thresholds: moving means of every frame, then the eccentricity and
+//    threshold of frames [0, fa) and [fb, P);
+//  * dirty: for those frames, whether the output can differ from the larger
+//    window's, given that window's thresholds at this window's offset
+//    (d_thr_union): some sample of the frame lies above one threshold and not
+//    the other, or -- with lo_edge / hi_edge, this window's first / last frame
+//    not being the larger window's -- the frame lies within the 5-frame
+//    smoothing stencil's reach of that end and has a sample above its
+//    threshold.  d_dirty gets one byte per frame of [0, P) (1 = can differ;
+//    frames [fa, fb) are 0);
+//  * output: the filtered frames [f0, f1) from the thresholds of the first
+//    step (every frame of [f0, f1) must lie in [0, fa) or [fb, P)).
+int launch_adaptive_filter_ends_thresholds(const struct recon_metadata &mr, const float *d_in, const float *d_sup,
+                                           float *d_scratch, int fa, int fb, cudaStream_t stream);
+int launch_adaptive_filter_dirty(const struct recon_metadata &mr, const float *d_sup, const float *d_thr_union,
+                                 const float *d_scratch, int fa, int fb, int lo_edge, int hi_edge,
+                                 unsigned char *d_dirty, cudaStream_t stream);
+int launch_adaptive_filter_output(const struct recon_metadata &mr, const float *d_in, float *d_out,
+                                  const float *d_sup, float *d_scratch, int f0, int f1, cudaStream_t stream);
 
 // The same filter over a window whose frames arrive in order: advance() is
 // told how many leading frames of d_in are present and launches every step
