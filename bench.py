@@ -867,13 +867,22 @@ def measure_fp16(args, torch, lib, m, ref):
     filter_rows = (sizes["union_rebin_samples"] // n)
     flop = 3 * 2.0 * n * n * filter_rows
     ramp_ms = stage_ms[2] / args.steps
+    peaks, peak_kind = measured_peaks()
+    peak_tc = peaks.get("bf16_tflops", 1900.0)
+    achieved_tc = flop / (ramp_ms * 1e-3) / 1e12
     out = {"value": sizes["vu_total"] / (ms * 1e-3), "unit": "voxel-updates/s", "ms_per_step": ms,
            "scans_per_s": 1e3 / ms,
            "stages_ms_per_step": {name: stage_ms[i] / args.steps for i, name in enumerate(STAGES)},
-           "ramp_filter_tensor": {"flop_per_union_pass": flop, "ms_per_step_incl_edge_views": ramp_ms,
-                                  "achieved_tflops_lower_bound": flop / (ramp_ms * 1e-3) / 1e12,
-                                  "note": "FP16 hi/lo products (3 per sample pair) of the union's rows; the "
-                                          "stage time also covers the edge views' rows and the row split"},
+           "roofline": {"kernel": "ramp_tc_gemm_kernel (with its row-split pass)", "bound": "tensor",
+                        "achieved": achieved_tc, "peak": peak_tc, "unit": "TFLOP/s", "frac": achieved_tc / peak_tc,
+                        "peak_source": "BF16 dense burst, MEASURED_PEAKS.json (%s); FP16 runs at the same "
+                                       "tensor rate" % peak_kind,
+                        "flop_per_row": 3 * 2.0 * n * n, "rows_per_step": filter_rows,
+                        "algorithmic_tflops": flop / 3 / (ramp_ms * 1e-3) / 1e12,
+                        "tensor_pipe_active_ncu": read_traffic().get("ramp_tc_tensor_pipe_active"),
+                        "note": "3 FP16 products (hi.hi, hi.lo, lo.hi) of 2 N_os^2 FLOP per row over the union's "
+                                "rows (algorithmic_tflops counts one); the stage time also covers the re-made "
+                                "edge views' rows and the row split, so achieved is a lower bound"},
            "max_hu_vs_fp32_path": float(diff.max()) * hu,
            "rms_hu_vs_fp32_path": float(diff.pow(2).mean().sqrt()) * hu,
            "entry_point": m["dev_entry"] + " after ctbb_set_storage(CTBB_STORAGE_FP16)"}
