@@ -1115,6 +1115,17 @@ struct TuneEntry {
 static std::mutex g_tune_mu;
 static std::map<TuneKey, TuneEntry> g_tuned;
 
+// Timed launches per candidate (the fastest counts): CTBB_TUNE_REPS, 1 to 9.
+static int tune_reps()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_TUNE_REPS");
+        const int r = e ? atoi(e) : 1;
+        return r < 1 ? 1 : (r > 9 ? 9 : r);
+    }();
+    return v;
+}
+
 static int tuned_shape(Context &c, const BpParams &p_any, const BpShape &fallback, BpShape *out)
 {
     const bool quad = p_any.vscale != nullptr;
@@ -1133,17 +1144,23 @@ static int tuned_shape(Context &c, const BpParams &p_any, const BpShape &fallbac
     double best_ms = 1e30;
     cudaEvent_t e0 = pooled_event(c), e1 = pooled_event(c);
     for (size_t k = 0; k < cand.size() && k < 8; ++k) {
+        if (cand[k].col && p_any.nht > kColumnMaxHalfTurns) continue;  // the window does not fit
         BpParams p = p_any;
+        p.col_zpt = cand[k].col ? cand[k].zpt : 0;
         p.warp_w = cand[k].warp_w;
         p.cta_w = std::max(cand[k].cta_w, p.warp_w);
         if (cand[k].threads / p.cta_w < 32 / p.warp_w) p.cta_w = (cand[k].threads / 32) * p.warp_w;
         CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));  // warm-up (module load, caches)
-        CTBB_CUDA_TRY(cudaEventRecord(e0, c.stream));
-        CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));
-        CTBB_CUDA_TRY(cudaEventRecord(e1, c.stream));
-        CTBB_CUDA_TRY(cudaEventSynchronize(e1));
-        float ms = 0.0f;
-        CTBB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        float ms = 1e30f;
+        for (int r = 0; r < tune_reps(); ++r) {
+            CTBB_CUDA_TRY(cudaEventRecord(e0, c.stream));
+            CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));
+            CTBB_CUDA_TRY(cudaEventRecord(e1, c.stream));
+            CTBB_CUDA_TRY(cudaEventSynchronize(e1));
+            float t = 0.0f;
+            CTBB_CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+            ms = std::min(ms, t);
+        }
         best.ms[k] = ms;
         best.n = (int)k + 1;
         if (ms < best_ms) {
@@ -1175,10 +1192,11 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
         const size_t n_block = mr->ri.n_slices_block;
         ScanPrep prep;
         CTBB_TRY(prepare_scan_device(c, mr, d_scan, &prep));
-        const BpShape fallback = c.storage ? BpShape{} : default_bp_shape(bp_zpt());
         for (size_t b = 0; b < prep.blocks.size(); ++b) {
             mr->ri = prep.blocks[b];
             float *slab = c.image.as<float>() + b * n_block * plane;
+            const BpShape fallback =
+                fit_bp_shape(default_bp_shape(bp_zpt(), c.storage != 0), prep.tables[b].nht);
             BpParams p;
             CTBB_TRY(prepared_block_params(c, *mr, prep, b, slab, fallback, &p));
             BpShape shape = fallback;
@@ -1271,11 +1289,11 @@ extern "C" int ctbb_batch_add_device(struct recon_metadata *mr, const float *d_s
         swap_slot(c, sl);
         int st = prepare_scan_device(c, mr, d_scan, &sl.prep);
         const size_t plane = (size_t)mr->rp.nx * mr->rp.ny;
-        const BpShape fallback = c.storage ? BpShape{} : default_bp_shape(8);
         std::vector<std::pair<BpShape, BpParams>> items;
         for (size_t b = 0; st == CTBB_OK && b < sl.prep.blocks.size(); ++b) {
             mr->ri = sl.prep.blocks[b];
             float *slab = c.image.as<float>() + b * mr->ri.n_slices_block * plane;
+            const BpShape fallback = fit_bp_shape(default_bp_shape(8, c.storage != 0), sl.prep.tables[b].nht);
             BpParams p;
             BpShape shape = fallback;
             st = prepared_block_params(c, *mr, sl.prep, b, slab, fallback, &p);
@@ -1359,14 +1377,17 @@ extern "C" int ctbb_autotune_report(char *buf, size_t n)
         const TuneKey &k = kv.first;
         const TuneEntry &e = kv.second;
         char line[512];
-        int len = snprintf(line, sizeof(line), "%dx%dx%d nos %d rows %d nht %d %s: zpt %d threads %d ctas/sm %d cta_w %d;",
-                           k.nx, k.ny, k.n_slices, k.nos, k.n_rows, k.nht, k.quad ? "fp16" : "fp32", e.shape.zpt,
-                           e.shape.threads, e.shape.min_blocks, e.shape.cta_w);
+        int len = snprintf(line, sizeof(line),
+                           "%dx%dx%d nos %d rows %d nht %d %s: %s zpt %d threads %d ctas/sm %d cta_w %d;", k.nx, k.ny,
+                           k.n_slices, k.nos, k.n_rows, k.nht, k.quad ? "fp16" : "fp32",
+                           e.shape.col ? "column" : "tile",
+                           e.shape.zpt, e.shape.threads, e.shape.min_blocks, e.shape.cta_w);
         out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
         const std::vector<BpShape> &cc = k.quad ? cqq : cq;
         for (int i = 0; i < e.n && i < (int)cc.size(); ++i) {
-            len = snprintf(line, sizeof(line), " %d/%d/%d/%d %.3f ms", cc[i].zpt, cc[i].threads, cc[i].min_blocks,
-                           cc[i].cta_w, e.ms[i]);
+            if (e.ms[i] <= 0.0) continue;  // not a candidate for this window
+            len = snprintf(line, sizeof(line), " %s%d/%d/%d/%d %.3f ms", cc[i].col ? "c" : "t", cc[i].zpt,
+                           cc[i].threads, cc[i].min_blocks, cc[i].cta_w, e.ms[i]);
             out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
         }
         out += "\n";

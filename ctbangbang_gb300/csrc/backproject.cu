@@ -19,9 +19,16 @@
 // interpolation) use FMA and reciprocals.  The reference's pi' = 3.1415368979f
 // is used where it uses it.
 //
-// GB300 mapping: one thread per (x, y) column and ZPT (8) consecutive
-// slices, 128-thread CTAs of 32 x 4 columns, each warp an 8 x 4 tile so that
-// its gathers fall on few detector channels.  Per angle i the asin and root
+// GB300 mapping.  Two forms share the arithmetic below.  The column form (the
+// default, backproject_column_tile) gives a thread the (x, y) column over up to
+// 32 slices: per angle it computes the geometry of each half turn once and
+// parks it in shared memory, then runs the slices in sub-chunks of 8, each
+// fetching all of a visit's footprints before it uses any (one wait on the
+// gathers per visit); 128-thread CTAs of 16 x 8 columns.  The slice-chunk form
+// (backproject_tile; windows of more than 8 half turns) gives a thread ZPT (8)
+// consecutive slices of a column, 128-thread CTAs of 32 x 4 columns.  In both
+// each warp is an 8 x 4 tile of columns so that its gathers fall on few
+// detector channels.  Per angle i the asin and root
 // of the k = 0 view are carried to every half turn to first order in |p|
 // (the reference's half turns are pi', not pi, apart), and a warp-uniform
 // window limits k to the half turns whose rays can reach the chunk.  Per visited (i, k) the geometry is computed once for the chunk,
@@ -445,6 +452,295 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
     backproject_tile<ZPT, NOS, THREADS, QUAD>(p, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// ---- column form --------------------------------------------------------
+// A thread owns the voxel column (x, y) over up to ZMAX slices (zpt of them,
+// in sub-chunks of kSub).  Per angle, the geometry of every half turn in the
+// column's window -- q of the first slice, its step per slice, the channel
+// weights and the footprint row address -- is computed once for all of the
+// column's slices and parked in shared memory (each thread its own entries,
+// no barrier).  Each sub-chunk then sums its visits with the per-angle sums of
+// its slices in registers and folds s / h into the image sums.  Against the
+// slice-chunk form above (geometry once per 8 slices) this divides the
+// per-visit geometry, the angle set-up and the window search by the number of
+// sub-chunks, for one shared-memory load per visit.
+//
+// Whether p_idx lies on the detector, and (FP16 footprint words) the view's
+// scale, are folded into the two channel weights: a sample whose p_idx is off
+// the detector then reads channel 0 of its view and adds exactly zero to s
+// while its weight still adds to h (interp2's rule).
+//
+// Geometry entry of half turn k (window slot kk) for thread tid:
+//   geo_w[kk][tid] = {q0, dq, (1 - wp) c, wp c}   c = [p on the detector] * scale
+//   geo_a[kk][tid] = address of the view's (ip, row 0) moved back as in row_floor
+template <int ZMAX, int SUB, int NOS, int THREADS, bool QUAD, class Params>
+__device__ __forceinline__ void backproject_column_tile(const Params &p, int bx, int by, int bz, float4 *geo_w,
+                                                        uint2 *geo_a)
+{
+    static_assert(ZMAX / SUB <= 4 && SUB % 2 == 0, "sub-chunk masks hold 4 sub-chunks per half turn");
+    constexpr unsigned kElem = QUAD ? sizeof(uint2) : sizeof(float);
+    const int nos = NOS > 0 ? NOS : p.nos;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tiles_x = p.cta_w / p.warp_w;
+    const int xi = bx * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
+    const int yi = by * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
+    const int zpt = p.col_zpt;
+    const int z0 = bz * zpt;
+    if (xi >= p.nx || yi >= p.ny) return;
+    const int nsub = (min(zpt, p.n_slices - z0) + SUB - 1) / SUB;
+    const float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
+    const float y = __fadd_rn(__fmul_rn(p.pix_y, __fsub_rn((float)yi, p.y_c)), p.y0);
+
+    __shared__ float2 img_sh[ZMAX / 2][THREADS];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    float2 *img = &img_sh[0][tid];
+#pragma unroll
+    for (int m = 0; m < ZMAX / 2; ++m) img[m * THREADS] = make_float2(0.0f, 0.0f);
+    float4 *gw = geo_w + tid;
+    uint2 *ga = geo_a + tid;
+
+    const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
+    const unsigned view_stride = (unsigned)(p.n_rows * nos);
+    const float p_max = (float)(nos - 2);
+    const float p_mid = 0.5f * p_max;
+    const float q_max_last = (float)(p.n_rows - 2);
+    const float hr = p.half_rows;
+    const float z_end = fmaf((float)(nsub * SUB - 1), p.coll, zbase);
+    const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
+    const unsigned lanes = __activemask();
+
+    for (int i = 0; i < p.n_half; ++i) {
+        const float4 *vt = p.views + (size_t)i * p.nht;
+        float inv_root, slope, a_off, root_off;
+        int k_lo = 0, k_hi = p.nht - 1;
+        {
+            // the angle's k = 0 view: asin and root carried to each half turn
+            // to first order (see backproject_tile)
+            const float4 t0 = __ldg(vt);
+            const float phat0 = __fsub_rn(__fmul_rn(x, t0.y), __fmul_rn(y, t0.z));
+            const float a_abs = fabsf(asin_fast(phat0 * p.inv_rf));
+            const float l2 = fmaf(-phat0, phat0, p.rf2);
+            inv_root = rsqrtf(l2);
+            const float root = l2 * inv_root;
+            const float p0_abs = fabsf(phat0);
+            slope = p0_abs * inv_root;
+            a_off = fmaf(-p0_abs, inv_root, a_abs);
+            root_off = fmaf(slope, p0_abs, root);
+            if (p.k_window) {
+                const float reach = fmaf(root + fabsf(fmaf(x, t0.z, y * t0.y)), p.tan_cone, a_abs * p.abs_zr);
+                const float lo = (z_lo - reach - t0.w) * p.inv_half_feed;
+                const float hi = (z_hi + reach - t0.w) * p.inv_half_feed;
+                k_lo = max(k_lo, (int)ceilf(fminf(lo, hi) - kWindowMargin));
+                k_hi = min(k_hi, (int)floorf(fmaxf(lo, hi) + kWindowMargin));
+            }
+        }
+        k_lo = __reduce_min_sync(lanes, k_lo);
+        k_hi = __reduce_max_sync(lanes, k_hi);
+        // the window's geometry, once for every slice of the column
+        for (int k = k_lo; k <= k_hi; ++k) {
+            const float4 t = __ldg(vt + k);
+            const float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
+            const float a_k = fmaf(fabsf(phat), inv_root, a_off);
+            const float root_k = fmaf(-slope, fabsf(phat), root_off);
+            const float zb_ray = fmaf(copysignf(a_k, phat), p.zrot_over_2pi, zbase - t.w);
+            const float lhat = root_k - x * t.z - y * t.y;
+            const float inv_den = __fdividef(1.0f, lhat * p.tan_cone);
+            float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
+            if (fabsf(p_idx - p_mid) > p_mid - kBorderBand) p_idx = p_index_exact(p, phat);
+            const bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
+            const int ip = p_ok ? (int)p_idx : 0;
+            const float wp = p_idx - (float)ip;
+            const unsigned row = __float_as_uint(t.x);
+            float c = p_ok ? 1.0f : 0.0f;
+            if constexpr (QUAD) c *= __ldg(p.vscale + (size_t)row * p.n_rows);
+            const uint64_t view_rows = p.rebin_rows + ((uint64_t)row * view_stride + (unsigned)ip) * kElem;
+            const int kk = k - k_lo;
+            const float q0 = zb_ray * inv_den, dq = p.coll * inv_den;
+            gw[kk * THREADS] = make_float4(q0, dq, (1.0f - wp) * c, wp * c);
+            ga[kk * THREADS] = make_uint2((unsigned)view_rows, (unsigned)(view_rows >> 32));
+        }
+        for (int sc = 0; sc < nsub; ++sc) {
+            float2 s2[SUB / 2], h2[SUB / 2];
+#pragma unroll
+            for (int m = 0; m < SUB / 2; ++m) {
+                s2[m] = make_float2(0.0f, 0.0f);
+                h2[m] = make_float2(0.0f, 0.0f);
+            }
+            int n_flat = 0;
+            const float zc = (float)(sc * SUB);
+            for (int k = k_lo; k <= k_hi; ++k) {
+                const int kk = k - k_lo;
+                const float4 g = gw[kk * THREADS];
+                const float dq = g.y;
+                // q of the sub-chunk's slices: q0c + m dq, m = 0 .. SUB - 1
+                const float q0c = fmaf(zc, dq, g.x);
+                const float q_endc = fmaf((float)(SUB - 1), dq, q0c);
+                // no slice of the sub-chunk inside |q| < 1 in any lane: nothing to add
+                if (__all_sync(lanes, q0c >= 1.0f || q_endc <= -1.0f)) continue;
+                const uint2 av = ga[kk * THREADS];
+                const uint64_t view_rows = ((uint64_t)av.y << 32) | av.x;
+                const bool last = (k == p.nht - 1);
+                const float2 wp2 = make_float2(g.w, g.w);
+                const float2 omwp2 = make_float2(g.z, g.z);
+                const float2 dq2 = make_float2(dq, dq), q02 = make_float2(q0c, q0c);
+                const float2 hr2 = make_float2(hr, hr);
+                auto pair_value = [&](float2 ql, float2 tr) -> float2 {
+                    float2 wq = sub2(ql, sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
+                    float a00, a01, a10, a11, b00, b01, b10, b11;
+                    fetch_footprint<QUAD>(view_rows, nos, tr.x, a00, a01, a10, a11);
+                    fetch_footprint<QUAD>(view_rows, nos, tr.y, b00, b01, b10, b11);
+                    float2 c0 = fma2(wp2, make_float2(a01, b01), mul2(omwp2, make_float2(a00, b00)));
+                    float2 c1 = fma2(wp2, make_float2(a11, b11), mul2(omwp2, make_float2(a10, b10)));
+                    return fma2(wq, sub2(c1, c0), c0);
+                };
+                auto pair_weight = [&](float2 q) -> float2 {
+                    float2 t = make_float2(fmaxf(fabsf(q.x) - kQ, 0.0f), fmaxf(fabsf(q.y) - kQ, 0.0f));
+                    float2 arg = mul2(t, make_float2(p.taper_scale, p.taper_scale));
+                    float2 cc = make_float2(__cosf(arg.x), __cosf(arg.y));
+                    return mul2(cc, cc);
+                };
+                // every footprint of the sub-chunk is fetched before any is used,
+                // so that a visit waits for its gathers once
+                float fp[SUB][4];
+                float2 wq2[SUB / 2];
+                auto fetch_all = [&](const float2 *ql) {
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) {
+                        const float2 tr = row_floor(ql[m]);
+                        wq2[m] = sub2(ql[m], sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
+                        fetch_footprint<QUAD>(view_rows, nos, tr.x, fp[2 * m][0], fp[2 * m][1], fp[2 * m][2],
+                                              fp[2 * m][3]);
+                        fetch_footprint<QUAD>(view_rows, nos, tr.y, fp[2 * m + 1][0], fp[2 * m + 1][1],
+                                              fp[2 * m + 1][2], fp[2 * m + 1][3]);
+                    }
+                };
+                auto fetched_value = [&](int m) -> float2 {
+                    float2 c0 = fma2(wp2, make_float2(fp[2 * m][1], fp[2 * m + 1][1]),
+                                     mul2(omwp2, make_float2(fp[2 * m][0], fp[2 * m + 1][0])));
+                    float2 c1 = fma2(wp2, make_float2(fp[2 * m][3], fp[2 * m + 1][3]),
+                                     mul2(omwp2, make_float2(fp[2 * m][2], fp[2 * m + 1][2])));
+                    return fma2(wq2[m], sub2(c1, c0), c0);
+                };
+                const float a_max = fmaxf(fabsf(q0c), fabsf(q_endc));
+                if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
+                    const float ql0 = fmaf(q0c, hr, hr);
+                    const float dql = dq * hr;
+                    const float2 ql02 = make_float2(ql0, ql0), dql2 = make_float2(dql, dql);
+                    float2 ql[SUB / 2];
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m)
+                        ql[m] = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
+                    fetch_all(ql);
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) s2[m] = add2(s2[m], fetched_value(m));
+                    ++n_flat;
+                    continue;
+                }
+                const bool inner =
+                    a_max < kInnerMax && (!last || fmaf(a_max, hr, hr) < q_max_last - kRowMargin);
+                if (__all_sync(lanes, inner)) {
+                    float2 ql[SUB / 2], q[SUB / 2];
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) {
+                        q[m] = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        ql[m] = fma2(q[m], hr2, hr2);
+                    }
+                    fetch_all(ql);
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) {
+                        float2 w = pair_weight(q[m]);
+                        h2[m] = add2(h2[m], w);
+                        s2[m] = fma2(w, fetched_value(m), s2[m]);
+                    }
+                    continue;
+                }
+                const float t_max = kFloorMagic + (float)(p.n_rows - 2);  // row R-2
+                const bool border = last && fmaf(q_endc, hr, hr) > q_max_last - kBorderBand;
+                if (__any_sync(lanes, border)) {
+                    // rare: rows near the last half turn's border, decided by the
+                    // reference's own q_idx (p_idx off the detector adds nothing)
+                    const bool p_ok = (g.z != 0.0f) || (g.w != 0.0f);
+                    const float4 t = __ldg(vt + k);
+                    const float phat = __fsub_rn(__fmul_rn(x, t.y), __fmul_rn(y, t.z));
+                    const float theta = __ldg(p.theta + (size_t)i * p.nht + k);
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) {
+                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
+                        float2 w = pair_weight(q);
+                        w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
+                        h2[m] = add2(h2[m], w);
+                        float2 ql = fma2(q, hr2, hr2);
+                        float2 tr = row_floor(ql);
+                        tr = make_float2(fminf(fmaxf(tr.x, kFloorMagic), t_max), fminf(fmaxf(tr.y, kFloorMagic), t_max));
+                        float2 v = pair_value(ql, tr);
+                        bool ok_x = p_ok && in_x, ok_y = p_ok && in_y;
+                        const int zs = z0 + sc * SUB + 2 * m;
+                        if (ok_x) {
+                            float d = ql.x - q_max_last;
+                            if (d > kBorderBand) ok_x = false;
+                            else if (d > -kBorderBand)
+                                ok_x = last_turn_sample_valid(p, x, y, theta, t.y, t.z, phat,
+                                                              __ldg(p.zpos + min(zs, p.n_slices - 1)), k);
+                        }
+                        if (ok_y) {
+                            float d = ql.y - q_max_last;
+                            if (d > kBorderBand) ok_y = false;
+                            else if (d > -kBorderBand)
+                                ok_y = last_turn_sample_valid(p, x, y, theta, t.y, t.z, phat,
+                                                              __ldg(p.zpos + min(zs + 1, p.n_slices - 1)), k);
+                        }
+                        s2[m] = fma2(make_float2(ok_x ? w.x : 0.0f, ok_y ? w.y : 0.0f), v, s2[m]);
+                    }
+                    continue;
+                }
+#pragma unroll
+                for (int m = 0; m < SUB / 2; ++m) {
+                    float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                    bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
+                    if (!__any_sync(lanes, in_x || in_y)) continue;
+                    float2 w = pair_weight(q);
+                    w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
+                    h2[m] = add2(h2[m], w);
+                    float2 ql = fma2(q, hr2, hr2);
+                    float2 tr = row_floor(ql);
+                    tr = make_float2(fminf(fmaxf(tr.x, kFloorMagic), t_max), fminf(fmaxf(tr.y, kFloorMagic), t_max));
+                    s2[m] = fma2(w, pair_value(ql, tr), s2[m]);
+                }
+                        }
+            const float nf = (float)n_flat;
+            float2 *im = img + sc * (SUB / 2) * THREADS;
+#pragma unroll
+            for (int m = 0; m < SUB / 2; ++m) {
+                float2 hz = add2(h2[m], make_float2(nf, nf));
+                float2 rh = make_float2(__fdividef(1.0f, fmaxf(hz.x, 1e-30f)), __fdividef(1.0f, fmaxf(hz.y, 1e-30f)));
+                im[m * THREADS] = fma2(s2[m], rh, im[m * THREADS]);
+            }
+        }
+    }
+    const size_t plane = (size_t)p.nx * p.ny;
+    for (int z = 0; z < nsub * SUB; ++z)
+        if (z0 + z < p.n_slices) {
+            float2 v = img[(z / 2) * THREADS];
+            p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = ((z & 1) ? v.y : v.x) * p.out_scale;
+        }
+}
+
+// Dynamic shared memory of the column form: a geometry entry (24 bytes) per
+// thread and half turn of the window (at most nht).
+__host__ __device__ constexpr size_t column_geo_bytes(int nht, int threads)
+{
+    return (size_t)nht * threads * (sizeof(float4) + sizeof(uint2));
+}
+
+template <int ZMAX, int SUB, int MIN_BLOCKS, int NOS, int THREADS, bool QUAD>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_column_kernel(BpParams p)
+{
+    extern __shared__ float4 col_dyn[];
+    float4 *geo_w = col_dyn;
+    uint2 *geo_a = reinterpret_cast<uint2 *>(col_dyn + (size_t)p.nht * THREADS);
+    backproject_column_tile<ZMAX, SUB, NOS, THREADS, QUAD>(p, blockIdx.x, blockIdx.y, blockIdx.z, geo_w, geo_a);
+}
+
 // The blocks of a batch -- blocks of any number of scans -- in one launch:
 // grid.x runs over the CTA tiles of every block in turn (tile_start[b] is the
 // first tile of block b, tile_start[n_blocks] the total); a CTA finds its
@@ -480,6 +776,45 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
     const unsigned gx = (unsigned)((sp.nx + sp.cta_w - 1) / sp.cta_w);
     const unsigned gy = (unsigned)((sp.ny + cta_h - 1) / cta_h);
     backproject_tile<ZPT, NOS, THREADS, QUAD>(sp, (int)(local % gx), (int)((local / gx) % gy), (int)(local / (gx * gy)));
+}
+
+// The column form over a batch's blocks (see backproject_batch_kernel); the
+// geometry entries are sized for the batch's largest window (max_nht).
+template <int ZMAX, int SUB, int MIN_BLOCKS, int NOS, int THREADS, bool QUAD>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
+    backproject_column_batch_kernel(const BpParams *__restrict__ params, const unsigned *__restrict__ tile_start,
+                                    int n_blocks, int max_nht)
+{
+    __shared__ BpParams sp;
+    __shared__ int s_block;
+    extern __shared__ float4 col_dyn[];
+    const unsigned tile = blockIdx.x;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        int lo = 0, hi = n_blocks - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(tile_start + mid) <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        s_block = lo;
+    }
+    __syncthreads();
+    const int b = s_block;
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(params + b);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+        for (int w = tid; w < (int)(sizeof(BpParams) / 4); w += THREADS) dst[w] = __ldg(src + w);
+    }
+    __syncthreads();
+    const unsigned local = tile - __ldg(tile_start + b);
+    const int cta_h = THREADS / sp.cta_w;
+    const unsigned gx = (unsigned)((sp.nx + sp.cta_w - 1) / sp.cta_w);
+    const unsigned gy = (unsigned)((sp.ny + cta_h - 1) / cta_h);
+    float4 *geo_w = col_dyn;
+    uint2 *geo_a = reinterpret_cast<uint2 *>(col_dyn + (size_t)max_nht * THREADS);
+    backproject_column_tile<ZMAX, SUB, NOS, THREADS, QUAD>(sp, (int)(local % gx), (int)((local / gx) % gy),
+                                                      (int)(local / (gx * gy)), geo_w, geo_a);
 }
 
 // Threads (voxel columns) per CTA of the backprojector: 256 or 128.
@@ -628,6 +963,7 @@ int make_backproject_params(const struct recon_metadata &mr, const BackprojectTa
         set_error("backproject: detector too small");
         return CTBB_ERR_ARGUMENT;
     }
+    p.col_zpt = (shape.col && t.nht <= kColumnMaxHalfTurns) ? shape.zpt : 0;
     p.warp_w = shape.warp_w;
     p.cta_w = std::max(shape.cta_w, p.warp_w);
     if (shape.threads / p.cta_w < 32 / p.warp_w) p.cta_w = (shape.threads / 32) * p.warp_w;  // whole warp tiles in y
@@ -685,8 +1021,51 @@ int with_shape(const BpShape &s, bool quad, bool batch, F &&f)
 
 }  // namespace
 
-BpShape default_bp_shape(int zpt)
+// Backprojector form: the column form unless CTBB_BP_FORM=tile.
+bool bp_column_form()
 {
+    static bool v = [] {
+        const char *e = getenv("CTBB_BP_FORM");
+        return !(e && strcmp(e, "tile") == 0);
+    }();
+    return v;
+}
+
+// Slices per thread of the column form (32; 16 or 8).
+int bp_column_zpt()
+{
+    static int v = [] {
+        const char *e = getenv("CTBB_BP_COL_ZPT");
+        int z = e ? atoi(e) : 32;
+        return (z == 8 || z == 16 || z == 32) ? z : 32;
+    }();
+    return v;
+}
+
+BpShape fit_bp_shape(const BpShape &s, int nht)
+{
+    if (!s.col || nht <= kColumnMaxHalfTurns) return s;
+    BpShape t;  // the slice-chunk form's default
+    t.cta_w = s.cta_w;
+    t.warp_w = s.warp_w;
+    return t;
+}
+
+BpShape default_bp_shape(int zpt, bool quad)
+{
+    if (bp_column_form()) {
+        BpShape s;
+        s.col = 1;
+        s.zpt = bp_column_zpt();
+        s.threads = 128;
+        const int mb = bp_min_blocks();
+        s.min_blocks = (s.zpt <= 16 && mb == 8) ? 8 : (mb == 6 ? 6 : 7);
+        // CTAs of 16 x 8 voxel columns unless CTBB_BP_CTA_W names the width
+        s.cta_w = getenv("CTBB_BP_CTA_W") ? bp_cta_width() : 16;
+        s.warp_w = bp_warp_width();
+        return s;
+    }
+    if (quad) return BpShape{};
     BpShape s;
     s.zpt = (zpt == 4 || zpt == 16) ? zpt : 8;
     s.threads = s.zpt == 8 ? bp_cta_threads() : 256;
@@ -697,11 +1076,58 @@ BpShape default_bp_shape(int zpt)
     return s;
 }
 
+// The column form's instances: 128-thread CTAs; at most 32 slices per thread
+// (7 or 6 CTAs per SM) or at most 16 (8 CTAs per SM, 64 registers).
+// f(ZMAX, SUB, MIN_BLOCKS).
+template <class F>
+int with_column_shape(const BpShape &s, F &&f)
+{
+    using std::integral_constant;
+    if (s.col && s.threads == 128 && (s.zpt == 8 || s.zpt == 16 || s.zpt == 32)) {
+        if (s.min_blocks == 7)
+            return f(integral_constant<int, 32>(), integral_constant<int, 8>(), integral_constant<int, 7>());
+        if (s.min_blocks == 6)
+            return f(integral_constant<int, 32>(), integral_constant<int, 8>(), integral_constant<int, 6>());
+        if (s.min_blocks == 8 && s.zpt <= 16)
+            return f(integral_constant<int, 16>(), integral_constant<int, 8>(), integral_constant<int, 8>());
+    }
+    set_error("backproject: no column-form kernel for %d slices per thread, %d threads, %d CTAs per SM", s.zpt,
+              s.threads, s.min_blocks);
+    return CTBB_ERR_ARGUMENT;
+}
+
 int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream)
 {
     const bool quad = p.vscale != nullptr;
     const dim3 grid = grid_of(p, shape);
     const dim3 block(32, shape.threads / 32);
+    if (shape.col) {
+        if (p.nht > kColumnMaxHalfTurns || p.col_zpt != shape.zpt) {
+            set_error("backproject: column form needs at most %d half turns (%d) and matching parameters",
+                      kColumnMaxHalfTurns, p.nht);
+            return CTBB_ERR_ARGUMENT;
+        }
+        const size_t smem = column_geo_bytes(p.nht, 128);
+        CTBB_TRY(with_column_shape(shape, [&](auto zm, auto sb, auto mb) -> int {
+            constexpr int ZM = decltype(zm)::value, SB = decltype(sb)::value, MB = decltype(mb)::value;
+            // at most 24 KB of geometry beside the image sums (16 KB at most):
+            // within the default 48 KB, no attribute needed
+            if (quad) {
+                if (p.nos == 1472) backproject_column_kernel<ZM, SB, MB, 1472, 128, true><<<grid, block, smem, stream>>>(p);
+                else backproject_column_kernel<ZM, SB, MB, 0, 128, true><<<grid, block, smem, stream>>>(p);
+            } else if (p.nos == 1472) {
+                backproject_column_kernel<ZM, SB, MB, 1472, 128, false><<<grid, block, smem, stream>>>(p);
+            } else if (p.nos == 1344) {
+                backproject_column_kernel<ZM, SB, MB, 1344, 128, false><<<grid, block, smem, stream>>>(p);
+            } else {
+                backproject_column_kernel<ZM, SB, MB, 0, 128, false><<<grid, block, smem, stream>>>(p);
+            }
+            return CTBB_OK;
+        }));
+        count_launch();
+        CTBB_CUDA_TRY(cudaGetLastError());
+        return CTBB_OK;
+    }
     CTBB_TRY(with_shape(shape, quad, false, [&](auto z, auto mb, auto t, auto q) -> int {
         constexpr int Z = decltype(z)::value, MB = decltype(mb)::value, T = decltype(t)::value;
         constexpr bool Q = decltype(q)::value;
@@ -719,8 +1145,7 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
                        float *d_block, int zpt, cudaStream_t stream, const float *d_vscale, const BpShape *shape)
 {
-    BpShape s = shape ? *shape : default_bp_shape(zpt);
-    if (d_vscale && !shape) s = BpShape{};  // FP16 footprint rows: the default shape
+    const BpShape s = fit_bp_shape(shape ? *shape : default_bp_shape(zpt, d_vscale != nullptr), t.nht);
     BpParams p;
     CTBB_TRY(make_backproject_params(mr, t, d_views, d_theta, d_zpos, d_rebin, d_block, d_vscale, s, &p));
     return launch_backproject_params(p, s, stream);
@@ -754,6 +1179,14 @@ int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape 
     }
     BpParams *d_params = static_cast<BpParams *>(d_buf);
     unsigned *d_start = reinterpret_cast<unsigned *>(d_params + blocks.size());
+    int max_nht = 0;
+    for (const BpParams &p : blocks) {
+        if (shape.col && (p.col_zpt != shape.zpt || p.nht > kColumnMaxHalfTurns)) {
+            set_error("backproject batch: a block's parameters do not fit the column form");
+            return CTBB_ERR_ARGUMENT;
+        }
+        max_nht = std::max(max_nht, p.nht);
+    }
     CTBB_CUDA_TRY(cudaMemcpyAsync(d_params, blocks.data(), blocks.size() * sizeof(BpParams), cudaMemcpyHostToDevice,
                                   stream));
     CTBB_CUDA_TRY(cudaMemcpyAsync(d_start, start.data(), start.size() * sizeof(unsigned), cudaMemcpyHostToDevice,
@@ -761,6 +1194,30 @@ int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape 
     const unsigned total = start.back();
     const dim3 block(32, shape.threads / 32);
     const int nos = blocks[0].nos, n = (int)blocks.size();
+    if (shape.col) {
+        const size_t smem = column_geo_bytes(max_nht, 128);
+        CTBB_TRY(with_column_shape(shape, [&](auto zm, auto sb, auto mb) -> int {
+            constexpr int ZM = decltype(zm)::value, SB = decltype(sb)::value, MB = decltype(mb)::value;
+            if (quad) {
+                if (nos == 1472)
+                    backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, true><<<total, block, smem, stream>>>(
+                        d_params, d_start, n, max_nht);
+                else
+                    backproject_column_batch_kernel<ZM, SB, MB, 0, 128, true><<<total, block, smem, stream>>>(
+                        d_params, d_start, n, max_nht);
+            } else if (nos == 1472) {
+                backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, false><<<total, block, smem, stream>>>(
+                    d_params, d_start, n, max_nht);
+            } else {
+                backproject_column_batch_kernel<ZM, SB, MB, 0, 128, false><<<total, block, smem, stream>>>(
+                    d_params, d_start, n, max_nht);
+            }
+            return CTBB_OK;
+        }));
+        count_launch();
+        CTBB_CUDA_TRY(cudaGetLastError());
+        return CTBB_OK;
+    }
     CTBB_TRY(with_shape(shape, quad, true, [&](auto z, auto mb, auto t, auto q) -> int {
         constexpr int Z = decltype(z)::value, MB = decltype(mb)::value, T = decltype(t)::value;
         constexpr bool Q = decltype(q)::value;
@@ -777,16 +1234,14 @@ int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape 
 
 std::vector<BpShape> backproject_shape_candidates(bool quad)
 {
+    // 128-thread CTAs are 32 x 4 (cta_w 32) or 16 x 8 (cta_w 16) voxel columns
     std::vector<BpShape> c;
-    if (quad) {
-        for (int w : {64, 32, 128}) c.push_back(BpShape{8, 128, 7, w, 8});
-        return c;
-    }
-    c.push_back(BpShape{8, 128, 7, 64, 8});
-    c.push_back(BpShape{8, 128, 7, 32, 8});
-    c.push_back(BpShape{8, 128, 7, 128, 8});
-    c.push_back(BpShape{8, 256, 4, 64, 8});
-    c.push_back(BpShape{16, 256, 3, 64, 8});
+    c.push_back(BpShape{32, 128, 7, 16, 8, 1});
+    c.push_back(BpShape{32, 128, 7, 32, 8, 1});
+    c.push_back(BpShape{16, 128, 8, 16, 8, 1});
+    c.push_back(BpShape{8, 128, 7, 16, 8, 0});
+    c.push_back(BpShape{8, 128, 7, 32, 8, 0});
+    if (!quad) c.push_back(BpShape{8, 256, 4, 64, 8, 0});
     return c;
 }
 

@@ -52,20 +52,31 @@ struct BpParams {
     float taper_scale;     // (pi'/2) / (1 - Q)
     float out_scale;       // 2 pi' / n_proj_turn
     int flat_path;         // R >= 8: rows of |q| <= Q never reach a border
+    int col_zpt;           // column form: slices per thread (a multiple of 8, at most 32)
 };
 
 // A launch shape: slices per thread, threads per CTA, CTAs per SM the kernel
-// is compiled for, voxel columns along x per CTA and per warp.
+// is compiled for, voxel columns along x per CTA and per warp, and the form:
+// col = 0 the slice-chunk form (zpt slices per thread share one visit's
+// geometry), col = 1 the column form (zpt = 8, 16 or 32 slices per thread in
+// sub-chunks of 8 share one angle's geometry; windows of at most
+// kColumnMaxHalfTurns half turns).
 struct BpShape {
-    int zpt = 8, threads = 128, min_blocks = 7, cta_w = 64, warp_w = 8;
+    int zpt = 8, threads = 128, min_blocks = 7, cta_w = 64, warp_w = 8, col = 0;
     bool operator==(const BpShape &o) const
     {
         return zpt == o.zpt && threads == o.threads && min_blocks == o.min_blocks && cta_w == o.cta_w &&
-               warp_w == o.warp_w;
+               warp_w == o.warp_w && col == o.col;
     }
 };
-// The shape the environment knobs (CTBB_BP_*) name for this slice count.
-BpShape default_bp_shape(int zpt);
+constexpr int kColumnMaxHalfTurns = 8;
+// The shape the environment knobs (CTBB_BP_*) name: the column form (unless
+// CTBB_BP_FORM=tile), else the slice-chunk form with zpt slices per thread
+// (FP16 footprint words: its default shape).
+BpShape default_bp_shape(int zpt, bool quad);
+// s, or the slice-chunk form's default where s is the column form and the
+// window of nht half turns is more than it holds.
+BpShape fit_bp_shape(const BpShape &s, int nht);
 // Shapes the autotuner times (those the batch kernel is compiled for).
 std::vector<BpShape> backproject_shape_candidates(bool quad);
 
