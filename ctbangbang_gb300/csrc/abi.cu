@@ -76,6 +76,7 @@ struct Context {
     DeviceBuffer raw_in, raw_filt, rebin, block, image, final_stack, scratch;
     // tables
     DeviceBuffer bp_views, bp_theta, bp_zpos, fin_offsets, fin_slices, fin_weights;
+    DeviceBuffer bp_partial;  // the backprojector's partial image sums (angle chunks)
     // whole-scan paths: one block window filtered with its own statistics,
     // and per frame of each block window whether that can differ from the union
     DeviceBuffer edge_raw, dirty;
@@ -308,6 +309,18 @@ struct ViewRows {
     }
 };
 
+// The context's buffer for the backprojector's partial image sums, sized for
+// a block of mr split into the most angle chunks a launch shape uses.
+static int partial_scratch(Context &c, const struct recon_metadata &mr, void **ptr, size_t *bytes)
+{
+    const size_t need =
+        (size_t)kMaxAngleChunks * mr.ri.n_slices_block * (size_t)mr.rp.nx * (size_t)mr.rp.ny * sizeof(float);
+    CTBB_TRY(c.bp_partial.ensure(need));
+    *ptr = c.bp_partial.ptr;
+    *bytes = c.bp_partial.bytes;
+    return CTBB_OK;
+}
+
 static int do_backproject(Context &c, const struct recon_metadata &mr, const float *d_rebin, float *d_block,
                           const ViewRows *rows = nullptr)
 {
@@ -319,9 +332,12 @@ static int do_backproject(Context &c, const struct recon_metadata &mr, const flo
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
     CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
     CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    void *part = nullptr;
+    size_t part_bytes = 0;
+    CTBB_TRY(partial_scratch(c, mr, &part, &part_bytes));
     StageScope scope(c, 3);
     return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
-                              d_rebin, d_block, bp_zpt(), c.stream);
+                              d_rebin, d_block, bp_zpt(), c.stream, nullptr, nullptr, part, part_bytes);
 }
 
 // The whole-scan paths' backprojection of one block from the context's rows:
@@ -336,10 +352,13 @@ static int backproject_scan_rows(Context &c, const struct recon_metadata &mr, fl
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
     CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
     CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    void *part = nullptr;
+    size_t part_bytes = 0;
+    CTBB_TRY(partial_scratch(c, mr, &part, &part_bytes));
     StageScope scope(c, 3);
     return launch_backproject(mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
                               reinterpret_cast<const float *>(c.quads.ptr), d_block, 8, c.stream,
-                              c.qscale.as<float>());
+                              c.qscale.as<float>(), nullptr, part, part_bytes);
 }
 
 // Ramp filter of rows [row0, row0 + n_lines) of the whole-scan rows buffer:
@@ -443,7 +462,7 @@ static void release_context(Context &c, bool device_sync, bool unbind)
     }
     for (DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                             &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
-                            &c.fin_weights, &c.edge_raw, &c.dirty})
+                            &c.fin_weights, &c.edge_raw, &c.dirty, &c.bp_partial})
         b->release();
     if (c.rebin_tables.base) cudaFree(c.rebin_tables.base);
     c.rebin_tables = DeviceRebinTables{};
@@ -589,9 +608,13 @@ extern "C" int ctbb_backproject_fp16_device(const struct recon_metadata *mr, con
     CTBB_TRY(upload(c.bp_views, t.views, c.stream));
     CTBB_TRY(upload(c.bp_theta, t.theta, c.stream));
     CTBB_TRY(upload(c.bp_zpos, t.zpos, c.stream));
+    void *part = nullptr;
+    size_t part_bytes = 0;
+    CTBB_TRY(partial_scratch(c, *mr, &part, &part_bytes));
     StageScope scope(c, 3);
     return launch_backproject(*mr, t, c.bp_views.as<float4>(), c.bp_theta.as<float>(), c.bp_zpos.as<float>(),
-                              static_cast<const float *>(d_quads), d_block, 8, c.stream, d_scale);
+                              static_cast<const float *>(d_quads), d_block, 8, c.stream, d_scale, nullptr, part,
+                              part_bytes);
 }
 
 extern "C" int ctbb_backproject_device(const struct recon_metadata *mr, const float *d_rebin, float *d_block)
@@ -1150,11 +1173,16 @@ static int tuned_shape(Context &c, const BpParams &p_any, const BpShape &fallbac
         p.warp_w = cand[k].warp_w;
         p.cta_w = std::max(cand[k].cta_w, p.warp_w);
         if (cand[k].threads / p.cta_w < 32 / p.warp_w) p.cta_w = (cand[k].threads / 32) * p.warp_w;
-        CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));  // warm-up (module load, caches)
+        const size_t part = backproject_partial_bytes(p, cand[k]);
+        if (part) CTBB_TRY(c.bp_partial.ensure(part));
+        auto launch = [&]() {
+            return launch_backproject_params(p, cand[k], c.stream, c.bp_partial.ptr, c.bp_partial.bytes);
+        };
+        CTBB_TRY(launch());  // warm-up (module load, caches)
         float ms = 1e30f;
         for (int r = 0; r < tune_reps(); ++r) {
             CTBB_CUDA_TRY(cudaEventRecord(e0, c.stream));
-            CTBB_TRY(launch_backproject_params(p, cand[k], c.stream));
+            CTBB_TRY(launch());
             CTBB_CUDA_TRY(cudaEventRecord(e1, c.stream));
             CTBB_CUDA_TRY(cudaEventSynchronize(e1));
             float t = 0.0f;
@@ -1204,8 +1232,10 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
                 CTBB_TRY(tuned_shape(c, p, fallback, &shape));
                 CTBB_TRY(prepared_block_params(c, *mr, prep, b, slab, shape, &p));
             }
+            const size_t part = backproject_partial_bytes(p, shape);
+            if (part) CTBB_TRY(c.bp_partial.ensure(part));
             StageScope scope(c, 3);
-            CTBB_TRY(launch_backproject_params(p, shape, c.stream));
+            CTBB_TRY(launch_backproject_params(p, shape, c.stream, c.bp_partial.ptr, c.bp_partial.bytes));
         }
         CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), d_final, mu_water));
         CTBB_CUDA_TRY(cudaStreamSynchronize(c.stream));
@@ -1382,12 +1412,16 @@ extern "C" int ctbb_autotune_report(char *buf, size_t n)
                            k.n_slices, k.nos, k.n_rows, k.nht, k.quad ? "fp16" : "fp32",
                            e.shape.col ? "column" : "tile",
                            e.shape.zpt, e.shape.threads, e.shape.min_blocks, e.shape.cta_w);
+        if (e.shape.col) {
+            out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
+            len = snprintf(line, sizeof(line), " angle chunks %d;", e.shape.achunks);
+        }
         out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
         const std::vector<BpShape> &cc = k.quad ? cqq : cq;
         for (int i = 0; i < e.n && i < (int)cc.size(); ++i) {
             if (e.ms[i] <= 0.0) continue;  // not a candidate for this window
-            len = snprintf(line, sizeof(line), " %s%d/%d/%d/%d %.3f ms", cc[i].col ? "c" : "t", cc[i].zpt,
-                           cc[i].threads, cc[i].min_blocks, cc[i].cta_w, e.ms[i]);
+            len = snprintf(line, sizeof(line), " %s%d/%d/%d/%d/a%d %.3f ms", cc[i].col ? "c" : "t", cc[i].zpt,
+                           cc[i].threads, cc[i].min_blocks, cc[i].cta_w, cc[i].achunks, e.ms[i]);
             out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
         }
         out += "\n";
@@ -2073,7 +2107,7 @@ static size_t context_device_bytes(const Context &c)
     for (const DeviceBuffer *b : {&c.raw_in, &c.raw_in2, &c.raw_filt, &c.rebin, &c.block, &c.image, &c.final_stack,
                                   &c.scratch, &c.bp_views, &c.bp_theta, &c.bp_zpos, &c.fin_offsets, &c.fin_slices,
                                   &c.fin_weights, &c.edge_raw, &c.dirty, &c.tc_work, &c.quads, &c.qscale,
-                                  &c.bp_tables})
+                                  &c.bp_tables, &c.bp_partial})
         n += b->bytes;
     return n + c.ramp.capacity * sizeof(float2);
 }

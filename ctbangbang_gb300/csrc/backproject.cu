@@ -484,7 +484,11 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
     const int xi = bx * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
     const int yi = by * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
     const int zpt = p.col_zpt;
-    const int z0 = bz * zpt;
+    const int n_zc = (p.n_slices + zpt - 1) / zpt;
+    const int ac = bz / n_zc;  // angle chunk: half-turn angles [i_begin, i_end)
+    const int z0 = (bz - ac * n_zc) * zpt;
+    const int i_begin = (int)(((long long)ac * p.n_half) / p.n_achunks);
+    const int i_end = (int)(((long long)(ac + 1) * p.n_half) / p.n_achunks);
     if (xi >= p.nx || yi >= p.ny) return;
     const int nsub = (min(zpt, p.n_slices - z0) + SUB - 1) / SUB;
     const float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
@@ -508,7 +512,7 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
     const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
     const unsigned lanes = __activemask();
 
-    for (int i = 0; i < p.n_half; ++i) {
+    for (int i = i_begin; i < i_end; ++i) {
         const float4 *vt = p.views + (size_t)i * p.nht;
         float inv_root, slope, a_off, root_off;
         int k_lo = 0, k_hi = p.nht - 1;
@@ -718,11 +722,32 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
         }
     }
     const size_t plane = (size_t)p.nx * p.ny;
+    const size_t pix = (size_t)yi * p.nx + xi;
+    if (p.partial) {
+        float *part = p.partial + (size_t)ac * p.n_slices * plane;
+        for (int z = 0; z < nsub * SUB; ++z)
+            if (z0 + z < p.n_slices) {
+                float2 v = img[(z / 2) * THREADS];
+                part[(size_t)(z0 + z) * plane + pix] = (z & 1) ? v.y : v.x;
+            }
+        return;
+    }
     for (int z = 0; z < nsub * SUB; ++z)
         if (z0 + z < p.n_slices) {
             float2 v = img[(z / 2) * THREADS];
-            p.out[(size_t)(z0 + z) * plane + (size_t)yi * p.nx + xi] = ((z & 1) ? v.y : v.x) * p.out_scale;
+            p.out[(size_t)(z0 + z) * plane + pix] = ((z & 1) ? v.y : v.x) * p.out_scale;
         }
+}
+
+// The angle chunks' partial sums of n voxels added in chunk order and scaled.
+__global__ void backproject_combine_kernel(const float *__restrict__ partial, float *__restrict__ out, size_t n,
+                                           int chunks, float scale)
+{
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+        float s = partial[v];
+        for (int c = 1; c < chunks; ++c) s += partial[(size_t)c * n + v];
+        out[v] = s * scale;
+    }
 }
 
 // Dynamic shared memory of the column form: a geometry entry (24 bytes) per
@@ -964,6 +989,8 @@ int make_backproject_params(const struct recon_metadata &mr, const BackprojectTa
         return CTBB_ERR_ARGUMENT;
     }
     p.col_zpt = (shape.col && t.nht <= kColumnMaxHalfTurns) ? shape.zpt : 0;
+    p.n_achunks = 1;
+    p.partial = nullptr;
     p.warp_w = shape.warp_w;
     p.cta_w = std::max(shape.cta_w, p.warp_w);
     if (shape.threads / p.cta_w < 32 / p.warp_w) p.cta_w = (shape.threads / 32) * p.warp_w;  // whole warp tiles in y
@@ -975,7 +1002,8 @@ namespace {
 dim3 grid_of(const BpParams &p, const BpShape &s)
 {
     const int cta_h = s.threads / p.cta_w;
-    return dim3((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + cta_h - 1) / cta_h, (p.n_slices + s.zpt - 1) / s.zpt);
+    return dim3((p.nx + p.cta_w - 1) / p.cta_w, (p.ny + cta_h - 1) / cta_h,
+                ((p.n_slices + s.zpt - 1) / s.zpt) * (s.col ? std::max(p.n_achunks, 1) : 1));
 }
 
 // Calls f(Z, MB, T, QUAD) with the compile-time instance of a launch shape;
@@ -1063,6 +1091,10 @@ BpShape default_bp_shape(int zpt, bool quad)
         // CTAs of 16 x 8 voxel columns unless CTBB_BP_CTA_W names the width
         s.cta_w = getenv("CTBB_BP_CTA_W") ? bp_cta_width() : 16;
         s.warp_w = bp_warp_width();
+        // the half-turn angles in 16 chunks unless CTBB_BP_ACHUNKS names 1-16
+        const char *a = getenv("CTBB_BP_ACHUNKS");
+        const int ach = a ? atoi(a) : 16;
+        s.achunks = (ach >= 1 && ach <= kMaxAngleChunks) ? ach : 16;
         return s;
     }
     if (quad) return BpShape{};
@@ -1096,8 +1128,23 @@ int with_column_shape(const BpShape &s, F &&f)
     return CTBB_ERR_ARGUMENT;
 }
 
-int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream)
+size_t backproject_partial_bytes(const BpParams &p, const BpShape &shape)
 {
+    if (!shape.col || shape.achunks <= 1) return 0;
+    return (size_t)shape.achunks * p.n_slices * p.nx * p.ny * sizeof(float);
+}
+
+int launch_backproject_params(const BpParams &p_in, const BpShape &shape, cudaStream_t stream, void *scratch,
+                              size_t scratch_bytes)
+{
+    BpParams p = p_in;
+    p.n_achunks = 1;
+    p.partial = nullptr;
+    const size_t part_bytes = backproject_partial_bytes(p, shape);
+    if (part_bytes && scratch && scratch_bytes >= part_bytes && shape.achunks <= p.n_half) {
+        p.n_achunks = shape.achunks;
+        p.partial = static_cast<float *>(scratch);
+    }
     const bool quad = p.vscale != nullptr;
     const dim3 grid = grid_of(p, shape);
     const dim3 block(32, shape.threads / 32);
@@ -1126,6 +1173,13 @@ int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStrea
         }));
         count_launch();
         CTBB_CUDA_TRY(cudaGetLastError());
+        if (p.partial) {
+            const size_t n = (size_t)p.n_slices * p.nx * p.ny;
+            const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
+            backproject_combine_kernel<<<blocks, 256, 0, stream>>>(p.partial, p.out, n, p.n_achunks, p.out_scale);
+            count_launch();
+            CTBB_CUDA_TRY(cudaGetLastError());
+        }
         return CTBB_OK;
     }
     CTBB_TRY(with_shape(shape, quad, false, [&](auto z, auto mb, auto t, auto q) -> int {
@@ -1143,12 +1197,13 @@ int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStrea
 
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
-                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale, const BpShape *shape)
+                       float *d_block, int zpt, cudaStream_t stream, const float *d_vscale, const BpShape *shape,
+                       void *scratch, size_t scratch_bytes)
 {
     const BpShape s = fit_bp_shape(shape ? *shape : default_bp_shape(zpt, d_vscale != nullptr), t.nht);
     BpParams p;
     CTBB_TRY(make_backproject_params(mr, t, d_views, d_theta, d_zpos, d_rebin, d_block, d_vscale, s, &p));
-    return launch_backproject_params(p, s, stream);
+    return launch_backproject_params(p, s, stream, scratch, scratch_bytes);
 }
 
 size_t backproject_batch_bytes(size_t n_blocks) { return n_blocks * sizeof(BpParams) + (n_blocks + 1) * 4 + 256; }
@@ -1236,12 +1291,13 @@ std::vector<BpShape> backproject_shape_candidates(bool quad)
 {
     // 128-thread CTAs are 32 x 4 (cta_w 32) or 16 x 8 (cta_w 16) voxel columns
     std::vector<BpShape> c;
-    c.push_back(BpShape{32, 128, 7, 16, 8, 1});
-    c.push_back(BpShape{32, 128, 7, 32, 8, 1});
-    c.push_back(BpShape{16, 128, 8, 16, 8, 1});
-    c.push_back(BpShape{8, 128, 7, 16, 8, 0});
+    c.push_back(BpShape{32, 128, 7, 16, 8, 1, 16});
+    c.push_back(BpShape{32, 128, 7, 32, 8, 1, 16});
+    c.push_back(BpShape{32, 128, 7, 16, 8, 1, 8});
+    c.push_back(BpShape{16, 128, 7, 16, 8, 1, 16});
+    c.push_back(BpShape{16, 128, 8, 16, 8, 1, 16});
+    c.push_back(BpShape{8, 128, 7, 16, 8, 1, 16});
     c.push_back(BpShape{8, 128, 7, 32, 8, 0});
-    if (!quad) c.push_back(BpShape{8, 256, 4, 64, 8, 0});
     return c;
 }
 

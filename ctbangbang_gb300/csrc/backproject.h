@@ -53,6 +53,8 @@ struct BpParams {
     float out_scale;       // 2 pi' / n_proj_turn
     int flat_path;         // R >= 8: rows of |q| <= Q never reach a border
     int col_zpt;           // column form: slices per thread (a multiple of 8, at most 32)
+    int n_achunks;         // column form: angle chunks (grid z = slice chunks x angle chunks)
+    float *partial;        // n_achunks > 1: [n_achunks][n_slices][ny][nx] unscaled image sums
 };
 
 // A launch shape: slices per thread, threads per CTA, CTAs per SM the kernel
@@ -61,15 +63,19 @@ struct BpParams {
 // geometry), col = 1 the column form (zpt = 8, 16 or 32 slices per thread in
 // sub-chunks of 8 share one angle's geometry; windows of at most
 // kColumnMaxHalfTurns half turns).
+// achunks (column form): the half-turn angles split into that many chunks,
+// each run by CTAs of its own that write unscaled partial image sums, which a
+// second kernel adds in chunk order (smaller CTA lifetimes: a shorter tail).
 struct BpShape {
-    int zpt = 8, threads = 128, min_blocks = 7, cta_w = 64, warp_w = 8, col = 0;
+    int zpt = 8, threads = 128, min_blocks = 7, cta_w = 64, warp_w = 8, col = 0, achunks = 1;
     bool operator==(const BpShape &o) const
     {
         return zpt == o.zpt && threads == o.threads && min_blocks == o.min_blocks && cta_w == o.cta_w &&
-               warp_w == o.warp_w && col == o.col;
+               warp_w == o.warp_w && col == o.col && achunks == o.achunks;
     }
 };
 constexpr int kColumnMaxHalfTurns = 8;
+constexpr int kMaxAngleChunks = 16;  // the most angle chunks a launch shape uses
 // The shape the environment knobs (CTBB_BP_*) name: the column form (unless
 // CTBB_BP_FORM=tile), else the slice-chunk form with zpt slices per thread
 // (FP16 footprint words: its default shape).
@@ -84,7 +90,12 @@ int build_backproject_tables(const struct recon_metadata &mr, BackprojectTables 
 int make_backproject_params(const struct recon_metadata &mr, const BackprojectTables &t, const float4 *d_views,
                             const float *d_theta, const float *d_zpos, const float *d_rebin, float *d_block,
                             const float *d_vscale, const BpShape &shape, BpParams *p);
-int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream);
+// scratch: device memory for the partial image sums of shape.achunks > 1
+// (backproject_partial_bytes); with less, the angles run as one chunk.
+int launch_backproject_params(const BpParams &p, const BpShape &shape, cudaStream_t stream, void *scratch = nullptr,
+                              size_t scratch_bytes = 0);
+// Bytes of partial image sums a launch of this shape needs (0: none).
+size_t backproject_partial_bytes(const BpParams &p, const BpShape &shape);
 // Device bytes launch_backproject_batch needs for n blocks' parameters.
 size_t backproject_batch_bytes(size_t n_blocks);
 // All blocks (of any scans; one row storage and row length) in one launch of
@@ -94,7 +105,7 @@ int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape 
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
                        const float4 *d_views, const float *d_theta, const float *d_zpos, const float *d_rebin,
                        float *d_block, int zpt, cudaStream_t stream, const float *d_vscale = nullptr,
-                       const BpShape *shape = nullptr);
+                       const BpShape *shape = nullptr, void *scratch = nullptr, size_t scratch_bytes = 0);
 // d_vscale non-null: d_rebin holds footprint quads [V][R][Nos][4] FP16 (the
 // reduced-storage rows, see ramp_tc.h) with view v's scale at d_vscale[v R].
 
