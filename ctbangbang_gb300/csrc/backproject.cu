@@ -188,15 +188,20 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
     float2 *img = &img_sh[0][tid];
 #pragma unroll
     for (int m = 0; m < ZPT / 2; ++m) img[m * THREADS] = make_float2(0.0f, 0.0f);
-    // slice z of the chunk sits at zbase + z * coll (the exact per-slice value
-    // is only needed by the border recheck and is read from zpos there)
-    const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
+    // Slice z of the block sits at zbase + z * coll, zbase the block's slice 0,
+    // and q of slice z is q0 + z dq with q0 that of slice 0: the same
+    // arithmetic whatever the launch shape, so that the |q| < 1 decisions (a
+    // jump in the result) do not depend on it.  The exact per-slice z is only
+    // needed by the border recheck and is read from zpos there.
+    const float zbase = __ldg(p.zpos);
+    const float z0f = (float)z0;
+    const float zchunk = fmaf(z0f, p.coll, zbase);
     const unsigned view_stride = (unsigned)(p.n_rows * nos);  // < 2^20
     const float p_max = (float)(nos - 2);
     const float p_mid = 0.5f * p_max;
     const float q_max_last = (float)(p.n_rows - 2);
-    const float z_end = fmaf((float)(ZPT - 1), p.coll, zbase);
-    const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
+    const float z_end = fmaf((float)(ZPT - 1), p.coll, zchunk);
+    const float z_lo = fminf(zchunk, z_end), z_hi = fmaxf(zchunk, z_end);
     const unsigned warp_lanes = __activemask();
 
     for (int i = 0; i < p.n_half; ++i) {
@@ -263,9 +268,10 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
             float inv_den = __fdividef(1.0f, lhat * p.tan_cone);
             float q0 = zb_ray * inv_den;
             float dq = p.coll * inv_den;
-            float q_end = fmaf((float)(ZPT - 1), dq, q0);
+            const float q_first = fmaf(z0f, dq, q0);
+            const float q_end = fmaf(z0f + (float)(ZPT - 1), dq, q0);
             // no slice of the chunk inside |q| < 1: nothing to add, not even weight
-            if (q0 >= 1.0f || q_end <= -1.0f) continue;
+            if (q_first >= 1.0f || q_end <= -1.0f) continue;
             // p and its border decision exactly as the reference rounds them
             float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
             // within the band of either border (|p_idx - p_mid| > p_mid - band; the
@@ -322,8 +328,8 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
             unsigned lanes = __activemask();
 #pragma unroll
             for (int sc = 0; sc < ZPT / SUB; ++sc) {
-                const float q0c = fmaf((float)(sc * SUB), dq, q0);
-                const float q_endc = fmaf((float)(sc * SUB + SUB - 1), dq, q0);
+                const float q0c = fmaf(z0f + (float)(sc * SUB), dq, q0);
+                const float q_endc = fmaf(z0f + (float)(sc * SUB + SUB - 1), dq, q0);
                 if (ZPT > SUB && __all_sync(lanes, q0c >= 1.0f || q_endc <= -1.0f)) continue;
                 float a_max = fmaxf(fabsf(q0c), fabsf(q_endc));
                 if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
@@ -334,7 +340,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
 #pragma unroll
                         for (int mm = 0; mm < SUB / 2; ++mm) {
                             const int m = sc * (SUB / 2) + mm;
-                            float2 ql = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
+                            float2 ql = fma2(make_float2(z0f + (float)(2 * m), z0f + (float)(2 * m + 1)), dql2, ql02);
                             if constexpr (QUAD) s2[m] = fma2(pair_value(ql, row_floor(ql)), vs2, s2[m]);
                             else s2[m] = add2(s2[m], pair_value(ql, row_floor(ql)));
                         }
@@ -348,7 +354,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
 #pragma unroll
                         for (int mm = 0; mm < SUB / 2; ++mm) {
                             const int m = sc * (SUB / 2) + mm;
-                            float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                            float2 q = fma2(make_float2(z0f + (float)(2 * m), z0f + (float)(2 * m + 1)), dq2, q02);
                             float2 w = pair_weight(q);
                             h2[m] = add2(h2[m], w);
                             float2 ql = fma2(q, hr2, hr2);
@@ -359,7 +365,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
 #pragma unroll
                         for (int mm = 0; mm < SUB / 2; ++mm) {
                             const int m = sc * (SUB / 2) + mm;
-                            float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                            float2 q = fma2(make_float2(z0f + (float)(2 * m), z0f + (float)(2 * m + 1)), dq2, q02);
                             h2[m] = add2(h2[m], pair_weight(q));
                         }
                     }
@@ -376,7 +382,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
 #pragma unroll
                     for (int mm = 0; mm < SUB / 2; ++mm) {
                         const int m = sc * (SUB / 2) + mm;
-                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        float2 q = fma2(make_float2(z0f + (float)(2 * m), z0f + (float)(2 * m + 1)), dq2, q02);
                         bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                         float2 w = pair_weight(q);
                         w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
@@ -409,7 +415,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
 #pragma unroll
                 for (int mm = 0; mm < SUB / 2; ++mm) {
                     const int m = sc * (SUB / 2) + mm;
-                    float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                    float2 q = fma2(make_float2(z0f + (float)(2 * m), z0f + (float)(2 * m + 1)), dq2, q02);
                     bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                     // a pair outside |q| < 1 in every lane adds nothing
                     if (!__any_sync(lanes, in_x || in_y)) continue;
@@ -453,6 +459,8 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
 }
 
 // ---- column form --------------------------------------------------------
+enum { kOutScaled = 0, kOutPartial = 1, kOutFirst = 2, kOutMiddle = 3, kOutLast = 4 };
+
 // A thread owns the voxel column (x, y) over up to ZMAX slices (zpt of them,
 // in sub-chunks of kSub).  Per angle, the geometry of every half turn in the
 // column's window -- q of the first slice, its step per slice, the channel
@@ -473,8 +481,16 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
 //   geo_w[kk][tid] = {q0, dq, (1 - wp) c, wp c}   c = [p on the detector] * scale
 //   geo_a[kk][tid] = address of the view's (ip, row 0) moved back as in row_floor
 template <int ZMAX, int SUB, int NOS, int THREADS, bool QUAD, class Params>
-__device__ __forceinline__ void backproject_column_tile(const Params &p, int bx, int by, int bz, float4 *geo_w,
-                                                        uint2 *geo_a)
+//
+// Angle chunk ac of n_ac runs half-turn angles [ac n_half / n_ac, (ac + 1)
+// n_half / n_ac); out_mode says where its image sums go:
+//   kOutScaled   out = sums * out_scale (one chunk)
+//   kOutPartial  partial[ac] = sums (a combine kernel adds the chunks)
+//   kOutFirst    out = sums               (the first of chunks run one after
+//   kOutMiddle   out = out + sums          another: the same additions, in the
+//   kOutLast     out = (out + sums) * out_scale   same order, as the combine)
+__device__ __forceinline__ void backproject_column_tile(const Params &p, int bx, int by, int bz, int ac, int n_ac,
+                                                        int out_mode, float4 *geo_w, uint2 *geo_a)
 {
     static_assert(ZMAX / SUB <= 4 && SUB % 2 == 0, "sub-chunk masks hold 4 sub-chunks per half turn");
     constexpr unsigned kElem = QUAD ? sizeof(uint2) : sizeof(float);
@@ -484,11 +500,9 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
     const int xi = bx * p.cta_w + (warp % tiles_x) * p.warp_w + lane % p.warp_w;
     const int yi = by * (THREADS / p.cta_w) + (warp / tiles_x) * (32 / p.warp_w) + lane / p.warp_w;
     const int zpt = p.col_zpt;
-    const int n_zc = (p.n_slices + zpt - 1) / zpt;
-    const int ac = bz / n_zc;  // angle chunk: half-turn angles [i_begin, i_end)
-    const int z0 = (bz - ac * n_zc) * zpt;
-    const int i_begin = (int)(((long long)ac * p.n_half) / p.n_achunks);
-    const int i_end = (int)(((long long)(ac + 1) * p.n_half) / p.n_achunks);
+    const int z0 = bz * zpt;
+    const int i_begin = (int)(((long long)ac * p.n_half) / n_ac);
+    const int i_end = (int)(((long long)(ac + 1) * p.n_half) / n_ac);
     if (xi >= p.nx || yi >= p.ny) return;
     const int nsub = (min(zpt, p.n_slices - z0) + SUB - 1) / SUB;
     const float x = __fadd_rn(__fmul_rn(p.pix_x, __fsub_rn((float)xi, p.x_c)), p.x0);
@@ -502,14 +516,18 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
     float4 *gw = geo_w + tid;
     uint2 *ga = geo_a + tid;
 
-    const float zbase = __ldg(p.zpos + min(z0, p.n_slices - 1));
+    // slice z of the block at zbase + z coll and its q at q0 + z dq, zbase and
+    // q0 those of the block's slice 0, z the slice's index in the block (the
+    // same arithmetic for every launch shape, see backproject_tile)
+    const float zbase = __ldg(p.zpos);
+    const float zchunk = fmaf((float)z0, p.coll, zbase);
     const unsigned view_stride = (unsigned)(p.n_rows * nos);
     const float p_max = (float)(nos - 2);
     const float p_mid = 0.5f * p_max;
     const float q_max_last = (float)(p.n_rows - 2);
     const float hr = p.half_rows;
-    const float z_end = fmaf((float)(nsub * SUB - 1), p.coll, zbase);
-    const float z_lo = fminf(zbase, z_end), z_hi = fmaxf(zbase, z_end);
+    const float z_end = fmaf((float)(nsub * SUB - 1), p.coll, zchunk);
+    const float z_lo = fminf(zchunk, z_end), z_hi = fmaxf(zchunk, z_end);
     const unsigned lanes = __activemask();
 
     for (int i = i_begin; i < i_end; ++i) {
@@ -570,14 +588,14 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                 h2[m] = make_float2(0.0f, 0.0f);
             }
             int n_flat = 0;
-            const float zc = (float)(sc * SUB);
+            const float zc = (float)(z0 + sc * SUB);  // the sub-chunk's first slice
             for (int k = k_lo; k <= k_hi; ++k) {
                 const int kk = k - k_lo;
                 const float4 g = gw[kk * THREADS];
                 const float dq = g.y;
-                // q of the sub-chunk's slices: q0c + m dq, m = 0 .. SUB - 1
+                // q of the sub-chunk's slices: q0 + (zc + m) dq, m = 0 .. SUB - 1
                 const float q0c = fmaf(zc, dq, g.x);
-                const float q_endc = fmaf((float)(SUB - 1), dq, q0c);
+                const float q_endc = fmaf(zc + (float)(SUB - 1), dq, g.x);
                 // no slice of the sub-chunk inside |q| < 1 in any lane: nothing to add
                 if (__all_sync(lanes, q0c >= 1.0f || q_endc <= -1.0f)) continue;
                 const uint2 av = ga[kk * THREADS];
@@ -585,7 +603,7 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                 const bool last = (k == p.nht - 1);
                 const float2 wp2 = make_float2(g.w, g.w);
                 const float2 omwp2 = make_float2(g.z, g.z);
-                const float2 dq2 = make_float2(dq, dq), q02 = make_float2(q0c, q0c);
+                const float2 dq2 = make_float2(dq, dq), q02 = make_float2(g.x, g.x);
                 const float2 hr2 = make_float2(hr, hr);
                 auto pair_value = [&](float2 ql, float2 tr) -> float2 {
                     float2 wq = sub2(ql, sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
@@ -626,13 +644,13 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                 };
                 const float a_max = fmaxf(fabsf(q0c), fabsf(q_endc));
                 if (__all_sync(lanes, p.flat_path && a_max <= kQ)) {
-                    const float ql0 = fmaf(q0c, hr, hr);
+                    const float ql0 = fmaf(g.x, hr, hr);
                     const float dql = dq * hr;
                     const float2 ql02 = make_float2(ql0, ql0), dql2 = make_float2(dql, dql);
                     float2 ql[SUB / 2];
 #pragma unroll
                     for (int m = 0; m < SUB / 2; ++m)
-                        ql[m] = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dql2, ql02);
+                        ql[m] = fma2(make_float2(zc + (float)(2 * m), zc + (float)(2 * m + 1)), dql2, ql02);
                     fetch_all(ql);
 #pragma unroll
                     for (int m = 0; m < SUB / 2; ++m) s2[m] = add2(s2[m], fetched_value(m));
@@ -645,7 +663,7 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                     float2 ql[SUB / 2], q[SUB / 2];
 #pragma unroll
                     for (int m = 0; m < SUB / 2; ++m) {
-                        q[m] = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        q[m] = fma2(make_float2(zc + (float)(2 * m), zc + (float)(2 * m + 1)), dq2, q02);
                         ql[m] = fma2(q[m], hr2, hr2);
                     }
                     fetch_all(ql);
@@ -668,7 +686,7 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                     const float theta = __ldg(p.theta + (size_t)i * p.nht + k);
 #pragma unroll
                     for (int m = 0; m < SUB / 2; ++m) {
-                        float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                        float2 q = fma2(make_float2(zc + (float)(2 * m), zc + (float)(2 * m + 1)), dq2, q02);
                         bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                         float2 w = pair_weight(q);
                         w = make_float2(in_x ? w.x : 0.0f, in_y ? w.y : 0.0f);
@@ -699,7 +717,7 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                 }
 #pragma unroll
                 for (int m = 0; m < SUB / 2; ++m) {
-                    float2 q = fma2(make_float2((float)(2 * m), (float)(2 * m + 1)), dq2, q02);
+                    float2 q = fma2(make_float2(zc + (float)(2 * m), zc + (float)(2 * m + 1)), dq2, q02);
                     bool in_x = fabsf(q.x) < 1.0f, in_y = fabsf(q.y) < 1.0f;
                     if (!__any_sync(lanes, in_x || in_y)) continue;
                     float2 w = pair_weight(q);
@@ -723,19 +741,18 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
     }
     const size_t plane = (size_t)p.nx * p.ny;
     const size_t pix = (size_t)yi * p.nx + xi;
-    if (p.partial) {
-        float *part = p.partial + (size_t)ac * p.n_slices * plane;
-        for (int z = 0; z < nsub * SUB; ++z)
-            if (z0 + z < p.n_slices) {
-                float2 v = img[(z / 2) * THREADS];
-                part[(size_t)(z0 + z) * plane + pix] = (z & 1) ? v.y : v.x;
-            }
-        return;
-    }
+    float *dst = out_mode == kOutPartial ? p.partial + (size_t)ac * p.n_slices * plane : p.out;
     for (int z = 0; z < nsub * SUB; ++z)
         if (z0 + z < p.n_slices) {
-            float2 v = img[(z / 2) * THREADS];
-            p.out[(size_t)(z0 + z) * plane + pix] = ((z & 1) ? v.y : v.x) * p.out_scale;
+            const float2 v2 = img[(z / 2) * THREADS];
+            const float v = (z & 1) ? v2.y : v2.x;
+            float *o = dst + (size_t)(z0 + z) * plane + pix;
+            switch (out_mode) {
+            case kOutScaled: *o = v * p.out_scale; break;
+            case kOutMiddle: *o = *o + v; break;
+            case kOutLast: *o = (*o + v) * p.out_scale; break;
+            default: *o = v;  // kOutPartial, kOutFirst
+            }
         }
 }
 
@@ -757,13 +774,19 @@ __host__ __device__ constexpr size_t column_geo_bytes(int nht, int threads)
     return (size_t)nht * threads * (sizeof(float4) + sizeof(uint2));
 }
 
+// grid z: slice chunks x angle chunks (p.n_achunks; more than one writes the
+// chunks' partial sums to p.partial)
 template <int ZMAX, int SUB, int MIN_BLOCKS, int NOS, int THREADS, bool QUAD>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_column_kernel(BpParams p)
 {
     extern __shared__ float4 col_dyn[];
     float4 *geo_w = col_dyn;
     uint2 *geo_a = reinterpret_cast<uint2 *>(col_dyn + (size_t)p.nht * THREADS);
-    backproject_column_tile<ZMAX, SUB, NOS, THREADS, QUAD>(p, blockIdx.x, blockIdx.y, blockIdx.z, geo_w, geo_a);
+    const int n_zc = (p.n_slices + p.col_zpt - 1) / p.col_zpt;
+    const int ac = blockIdx.z / n_zc;
+    backproject_column_tile<ZMAX, SUB, NOS, THREADS, QUAD>(p, blockIdx.x, blockIdx.y, blockIdx.z - ac * n_zc, ac,
+                                                           p.n_achunks, p.partial ? kOutPartial : kOutScaled,
+                                                           geo_w, geo_a);
 }
 
 // The blocks of a batch -- blocks of any number of scans -- in one launch:
@@ -808,7 +831,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 template <int ZMAX, int SUB, int MIN_BLOCKS, int NOS, int THREADS, bool QUAD>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
     backproject_column_batch_kernel(const BpParams *__restrict__ params, const unsigned *__restrict__ tile_start,
-                                    int n_blocks, int max_nht)
+                                    int n_blocks, int max_nht, int ac, int n_ac)
 {
     __shared__ BpParams sp;
     __shared__ int s_block;
@@ -838,8 +861,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
     const unsigned gy = (unsigned)((sp.ny + cta_h - 1) / cta_h);
     float4 *geo_w = col_dyn;
     uint2 *geo_a = reinterpret_cast<uint2 *>(col_dyn + (size_t)max_nht * THREADS);
+    const int mode = n_ac == 1 ? kOutScaled : ac == 0 ? kOutFirst : ac == n_ac - 1 ? kOutLast : kOutMiddle;
     backproject_column_tile<ZMAX, SUB, NOS, THREADS, QUAD>(sp, (int)(local % gx), (int)((local / gx) % gy),
-                                                      (int)(local / (gx * gy)), geo_w, geo_a);
+                                                           (int)(local / (gx * gy)), ac, n_ac, mode, geo_w, geo_a);
 }
 
 // Threads (voxel columns) per CTA of the backprojector: 256 or 128.
@@ -1250,27 +1274,34 @@ int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape 
     const dim3 block(32, shape.threads / 32);
     const int nos = blocks[0].nos, n = (int)blocks.size();
     if (shape.col) {
+        // the angle chunks one launch after another, each over every block's
+        // tiles, each adding to the blocks' images (the CTAs in flight then
+        // share a chunk's views)
+        int n_ac = std::max(1, shape.achunks);
+        for (const BpParams &p : blocks) n_ac = std::min(n_ac, p.n_half);
         const size_t smem = column_geo_bytes(max_nht, 128);
-        CTBB_TRY(with_column_shape(shape, [&](auto zm, auto sb, auto mb) -> int {
-            constexpr int ZM = decltype(zm)::value, SB = decltype(sb)::value, MB = decltype(mb)::value;
-            if (quad) {
-                if (nos == 1472)
-                    backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, true><<<total, block, smem, stream>>>(
-                        d_params, d_start, n, max_nht);
-                else
-                    backproject_column_batch_kernel<ZM, SB, MB, 0, 128, true><<<total, block, smem, stream>>>(
-                        d_params, d_start, n, max_nht);
-            } else if (nos == 1472) {
-                backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, false><<<total, block, smem, stream>>>(
-                    d_params, d_start, n, max_nht);
-            } else {
-                backproject_column_batch_kernel<ZM, SB, MB, 0, 128, false><<<total, block, smem, stream>>>(
-                    d_params, d_start, n, max_nht);
-            }
-            return CTBB_OK;
-        }));
-        count_launch();
-        CTBB_CUDA_TRY(cudaGetLastError());
+        for (int ac = 0; ac < n_ac; ++ac) {
+            CTBB_TRY(with_column_shape(shape, [&](auto zm, auto sb, auto mb) -> int {
+                constexpr int ZM = decltype(zm)::value, SB = decltype(sb)::value, MB = decltype(mb)::value;
+                if (quad) {
+                    if (nos == 1472)
+                        backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, true><<<total, block, smem, stream>>>(
+                            d_params, d_start, n, max_nht, ac, n_ac);
+                    else
+                        backproject_column_batch_kernel<ZM, SB, MB, 0, 128, true><<<total, block, smem, stream>>>(
+                            d_params, d_start, n, max_nht, ac, n_ac);
+                } else if (nos == 1472) {
+                    backproject_column_batch_kernel<ZM, SB, MB, 1472, 128, false><<<total, block, smem, stream>>>(
+                        d_params, d_start, n, max_nht, ac, n_ac);
+                } else {
+                    backproject_column_batch_kernel<ZM, SB, MB, 0, 128, false><<<total, block, smem, stream>>>(
+                        d_params, d_start, n, max_nht, ac, n_ac);
+                }
+                return CTBB_OK;
+            }));
+            count_launch();
+            CTBB_CUDA_TRY(cudaGetLastError());
+        }
         return CTBB_OK;
     }
     CTBB_TRY(with_shape(shape, quad, true, [&](auto z, auto mb, auto t, auto q) -> int {
