@@ -1029,10 +1029,13 @@ def run_ours(args):
         },
         "hu": hu,
         "fp16_storage": fp16,
-        "roofline": {"kernel": "backproject_kernel", "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
+        "roofline": {"kernel": "backproject_column_kernel (with its angle-chunk combine)", "bound": "fp32",
+                     "achieved": achieved, "peak": peak_fp32,
                      "unit": "TFLOP/s", "frac": achieved / peak_fp32 if peak_fp32 > 0 else None,
                      "traffic": traffic, "flop_per_vu": FLOP_PER_VU, "vu_per_launch": vu_per_launch,
                      "launch_ms": bp_launch_ms,
+                     "launch_ms_note": "CUDA events around each block's backprojection: the column kernel and "
+                                       "the combine of its 16 angle chunks",
                      "peak_source": "measured FFMA-loop throughput of this GPU in this run "
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "stages": stages,

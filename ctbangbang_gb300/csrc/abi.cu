@@ -1420,8 +1420,8 @@ extern "C" int ctbb_autotune_report(char *buf, size_t n)
         const std::vector<BpShape> &cc = k.quad ? cqq : cq;
         for (int i = 0; i < e.n && i < (int)cc.size(); ++i) {
             if (e.ms[i] <= 0.0) continue;  // not a candidate for this window
-            len = snprintf(line, sizeof(line), " %s%d/%d/%d/%d/a%d %.3f ms", cc[i].col ? "c" : "t", cc[i].zpt,
-                           cc[i].threads, cc[i].min_blocks, cc[i].cta_w, cc[i].achunks, e.ms[i]);
+            len = snprintf(line, sizeof(line), " %s%d/%d/%d/%dx%d/a%d %.3f ms", cc[i].col ? "c" : "t", cc[i].zpt,
+                           cc[i].threads, cc[i].min_blocks, cc[i].cta_w, cc[i].warp_w, cc[i].achunks, e.ms[i]);
             out.append(line, (size_t)std::max(0, std::min(len, (int)sizeof(line) - 1)));
         }
         out += "\n";

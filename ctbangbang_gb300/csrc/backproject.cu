@@ -1327,7 +1327,6 @@ std::vector<BpShape> backproject_shape_candidates(bool quad)
     c.push_back(BpShape{32, 128, 7, 16, 8, 1, 8});
     c.push_back(BpShape{16, 128, 7, 16, 8, 1, 16});
     c.push_back(BpShape{16, 128, 8, 16, 8, 1, 16});
-    c.push_back(BpShape{8, 128, 7, 16, 8, 1, 16});
     c.push_back(BpShape{8, 128, 7, 32, 8, 0});
     return c;
 }
