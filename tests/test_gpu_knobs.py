@@ -1,7 +1,8 @@
 """GPU tests of the environment knobs (read once per process, so each setting
 runs in its own process): the streamed whole-scan path gives the device
 path's stack bit for bit at any number of copy chunks, and the
-backprojector's launch shapes agree with the default to rounding."""
+backprojector's forms and launch shapes agree with the default to
+rounding."""
 import ctypes as C
 import os
 import subprocess
@@ -64,16 +65,25 @@ def test_streamed_path_any_chunk_count(torch_cuda, tmp_path):
 
 
 def test_backprojector_launch_shapes_agree(torch_cuda, tmp_path):
-    """Other CTA / warp tilings, CTA sizes and slices per thread change which
-    chunks a warp classes as flat, inner or other (whose row coordinates round
-    differently) and where slice chunks start, not the algorithm: within
-    0.01 HU of the default."""
+    """Both backprojector forms and their launch shapes against the default
+    (column form, 32 slices per thread, 16 angle chunks): other CTA / warp
+    tilings, slices per thread and angle chunks change which sub-chunks a warp
+    classes as flat, inner or other (whose row coordinates round differently)
+    and the order of the angle sums, not the algorithm -- and since q of every
+    slice is taken from the block's slice 0 in every form, not the |q| < 1
+    decisions either: within 0.01 HU of the default."""
     want = run_child(tmp_path, "default", {})
     hu = 1000.0 / 0.019
-    for name, env in (("w4c32", {"CTBB_BP_WARP_W": "4", "CTBB_BP_CTA_W": "32"}),
-                      ("w32", {"CTBB_BP_WARP_W": "32"}),
-                      ("t256", {"CTBB_BP_THREADS": "256", "CTBB_BP_MINB": "4"}),
-                      ("z16", {"CTBB_BP_ZPT": "16"})):
+    for name, env in (("a1", {"CTBB_BP_ACHUNKS": "1"}),
+                      ("a4", {"CTBB_BP_ACHUNKS": "4"}),
+                      ("z16", {"CTBB_BP_COL_ZPT": "16"}),
+                      ("z16m8", {"CTBB_BP_COL_ZPT": "16", "CTBB_BP_MINB": "8"}),
+                      ("z8", {"CTBB_BP_COL_ZPT": "8"}),
+                      ("c32", {"CTBB_BP_CTA_W": "32"}),
+                      ("w4c32", {"CTBB_BP_WARP_W": "4", "CTBB_BP_CTA_W": "32"}),
+                      ("tile", {"CTBB_BP_FORM": "tile"}),
+                      ("tile_t256", {"CTBB_BP_FORM": "tile", "CTBB_BP_THREADS": "256", "CTBB_BP_MINB": "4"}),
+                      ("tile_z16", {"CTBB_BP_FORM": "tile", "CTBB_BP_ZPT": "16"})):
         got = run_child(tmp_path, name, env)
         diff = np.abs((got.astype(np.float64) - want) * hu).max()
         print("launch shape %s: max %.2e HU from the default" % (name, diff))
