@@ -280,7 +280,7 @@ __device__ __forceinline__ void backproject_tile(const Params &p, int bx, int by
             if (fabsf(p_idx - p_mid) > p_mid - kBorderBand) p_idx = p_index_exact(p, phat);
             bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
             bool last = (k == p.nht - 1);
-            int ip = p_ok ? (int)p_idx : 0;
+            int ip = p_ok ? (int)p_idx : (p_idx < 0.0f ? 0 : nos - 2);
             float wp = p_idx - (float)ip;
             const uint64_t view_rows =
                 p.rebin_rows + ((uint64_t)__float_as_uint(t.x) * view_stride + (unsigned)ip) * kElem;
@@ -569,7 +569,9 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
             float p_idx = fmaf(phat, p.inv_ds_half, p.two_cc);
             if (fabsf(p_idx - p_mid) > p_mid - kBorderBand) p_idx = p_index_exact(p, phat);
             const bool p_ok = (p_idx >= 0.0f) && (p_idx <= p_max);
-            const int ip = p_ok ? (int)p_idx : 0;
+            // off the detector: the nearest edge channel (its weight is zero;
+            // the address stays near the warp's other lanes' lines)
+            const int ip = p_ok ? (int)p_idx : (p_idx < 0.0f ? 0 : nos - 2);
             const float wp = p_idx - (float)ip;
             const unsigned row = __float_as_uint(t.x);
             float c = p_ok ? 1.0f : 0.0f;
@@ -605,6 +607,30 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                 const float2 omwp2 = make_float2(g.z, g.z);
                 const float2 dq2 = make_float2(dq, dq), q02 = make_float2(g.x, g.x);
                 const float2 hr2 = make_float2(hr, hr);
+                // cos^2 taper weight of a pair: W = 1 below Q (cos(0) = 1), then
+                // cos^2(pi/2 (|q| - Q) / (1 - Q))
+                auto pair_weight = [&](float2 q) -> float2 {
+                    float2 t = make_float2(fmaxf(fabsf(q.x) - kQ, 0.0f), fmaxf(fabsf(q.y) - kQ, 0.0f));
+                    float2 arg = mul2(t, make_float2(p.taper_scale, p.taper_scale));
+                    float2 cc = make_float2(__cosf(arg.x), __cosf(arg.y));
+                    return mul2(cc, cc);
+                };
+                // p off the detector in every lane: interp2 gives 0, so only the
+                // weights count (h), nothing is fetched
+                if (!__any_sync(lanes, (g.z != 0.0f) || (g.w != 0.0f))) {
+                    const float a_max0 = fmaxf(fabsf(q0c), fabsf(q_endc));
+                    if (__all_sync(lanes, a_max0 <= kQ)) {
+                        ++n_flat;
+                        continue;
+                    }
+#pragma unroll
+                    for (int m = 0; m < SUB / 2; ++m) {
+                        const float2 q = fma2(make_float2(zc + (float)(2 * m), zc + (float)(2 * m + 1)), dq2, q02);
+                        const float2 w = pair_weight(q);
+                        h2[m] = add2(h2[m], make_float2(fabsf(q.x) < 1.0f ? w.x : 0.0f, fabsf(q.y) < 1.0f ? w.y : 0.0f));
+                    }
+                    continue;
+                }
                 auto pair_value = [&](float2 ql, float2 tr) -> float2 {
                     float2 wq = sub2(ql, sub2(tr, make_float2(kFloorMagic, kFloorMagic)));
                     float a00, a01, a10, a11, b00, b01, b10, b11;
@@ -613,12 +639,6 @@ __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx,
                     float2 c0 = fma2(wp2, make_float2(a01, b01), mul2(omwp2, make_float2(a00, b00)));
                     float2 c1 = fma2(wp2, make_float2(a11, b11), mul2(omwp2, make_float2(a10, b10)));
                     return fma2(wq, sub2(c1, c0), c0);
-                };
-                auto pair_weight = [&](float2 q) -> float2 {
-                    float2 t = make_float2(fmaxf(fabsf(q.x) - kQ, 0.0f), fmaxf(fabsf(q.y) - kQ, 0.0f));
-                    float2 arg = mul2(t, make_float2(p.taper_scale, p.taper_scale));
-                    float2 cc = make_float2(__cosf(arg.x), __cosf(arg.y));
-                    return mul2(cc, cc);
                 };
                 // every footprint of the sub-chunk is fetched before any is used,
                 // so that a visit waits for its gathers once
