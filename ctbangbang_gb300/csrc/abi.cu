@@ -642,13 +642,15 @@ extern "C" size_t ctbb_workspace_bytes(const struct recon_metadata *mr)
 {
     if (check_mr(mr)) return 0;
     BlockDims d = block_dims(*mr);
-    // raw window (copy) + filtered raw + rebin + image stack; pull windows of
+    // raw window (copy) + filtered raw + rebin + image stack + the
+    // backprojector's angle-chunk partial sums of a block; pull windows of
     // later blocks can be up to 128 frames longer than the planned first one.
     size_t frame = d.n_rows_raw * d.n_channels;
     size_t raw = (d.n_proj_pull + 256) * frame * sizeof(float);
     size_t rebin = ((d.n_proj_pull + 256) / d.n_ffs) * d.n_rows * d.n_os * sizeof(float);
     size_t image = (size_t)mr->rp.nx * mr->rp.ny * mr->ri.n_slices_recon * sizeof(float);
-    return 2 * raw + rebin + image;
+    size_t partial = (size_t)kMaxAngleChunks * mr->rp.nx * mr->rp.ny * mr->ri.n_slices_block * sizeof(float);
+    return 2 * raw + rebin + image + partial;
 }
 
 // Runs a reconstruction body and then waits for the context's copy and
@@ -941,8 +943,9 @@ static int run_edge_patch(Context &c, const struct recon_metadata &mb, const Reb
 
 // Device bytes the whole-scan paths (scan_device / scan_host / scan_file)
 // hold for this plan: the union window raw and filtered, its rebinned rows,
-// the adaptive filter's statistics, the image and final stacks, plus 8 MiB
-// for tables and staging slack.  0 if the plan is not usable.
+// the adaptive filter's statistics, the image and final stacks, the
+// backprojector's angle-chunk partial sums of a block, plus 8 MiB for tables
+// and staging slack.  0 if the plan is not usable.
 extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
 {
     if (!mr || check_mr(mr) || !mr->table_positions) return 0;
@@ -960,7 +963,8 @@ extern "C" size_t ctbb_scan_workspace_bytes(const struct recon_metadata *mr)
     return (2 * dg.raw_elems() + dg.rebin_elems() + sum_patch * view_elems + max_pull * frame +
             adaptive_filter_scratch_floats(dg.n_proj_pull) +
             adaptive_filter_scratch_floats(std::max(max_pull, sum_edge_pull)) + plane * mr->ri.n_slices_recon +
-            plane * (size_t)(n_final > 0 ? n_final : 1)) * sizeof(float) +
+            plane * (size_t)(n_final > 0 ? n_final : 1) +
+            (size_t)kMaxAngleChunks * mr->ri.n_slices_block * plane) * sizeof(float) +
            sum_edge_pull + ((size_t)8 << 20);
 }
 
