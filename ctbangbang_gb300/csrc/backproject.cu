@@ -462,9 +462,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) backproject_kernel(BpPara
 enum { kOutScaled = 0, kOutPartial = 1, kOutFirst = 2, kOutMiddle = 3, kOutLast = 4 };
 
 // A thread owns the voxel column (x, y) over up to ZMAX slices (zpt of them,
-// in sub-chunks of kSub).  Per angle, the geometry of every half turn in the
-// column's window -- q of the first slice, its step per slice, the channel
-// weights and the footprint row address -- is computed once for all of the
+// in sub-chunks of SUB = 8).  Per angle, the geometry of every half turn in
+// the column's window -- q of the block's slice 0, its step per slice, the
+// channel weights and the footprint row address -- is computed once for all of the
 // column's slices and parked in shared memory (each thread its own entries,
 // no barrier).  Each sub-chunk then sums its visits with the per-angle sums of
 // its slices in registers and folds s / h into the image sums.  Against the
@@ -474,13 +474,13 @@ enum { kOutScaled = 0, kOutPartial = 1, kOutFirst = 2, kOutMiddle = 3, kOutLast 
 //
 // Whether p_idx lies on the detector, and (FP16 footprint words) the view's
 // scale, are folded into the two channel weights: a sample whose p_idx is off
-// the detector then reads channel 0 of its view and adds exactly zero to s
-// while its weight still adds to h (interp2's rule).
+// the detector then reads the nearest edge channel of its view and adds
+// exactly zero to s while its weight still adds to h (interp2's rule); a visit
+// with p off the detector in every lane fetches nothing.
 //
 // Geometry entry of half turn k (window slot kk) for thread tid:
 //   geo_w[kk][tid] = {q0, dq, (1 - wp) c, wp c}   c = [p on the detector] * scale
 //   geo_a[kk][tid] = address of the view's (ip, row 0) moved back as in row_floor
-template <int ZMAX, int SUB, int NOS, int THREADS, bool QUAD, class Params>
 //
 // Angle chunk ac of n_ac runs half-turn angles [ac n_half / n_ac, (ac + 1)
 // n_half / n_ac); out_mode says where its image sums go:
@@ -489,10 +489,11 @@ template <int ZMAX, int SUB, int NOS, int THREADS, bool QUAD, class Params>
 //   kOutFirst    out = sums               (the first of chunks run one after
 //   kOutMiddle   out = out + sums          another: the same additions, in the
 //   kOutLast     out = (out + sums) * out_scale   same order, as the combine)
+template <int ZMAX, int SUB, int NOS, int THREADS, bool QUAD, class Params>
 __device__ __forceinline__ void backproject_column_tile(const Params &p, int bx, int by, int bz, int ac, int n_ac,
                                                         int out_mode, float4 *geo_w, uint2 *geo_a)
 {
-    static_assert(ZMAX / SUB <= 4 && SUB % 2 == 0, "sub-chunk masks hold 4 sub-chunks per half turn");
+    static_assert(SUB % 2 == 0 && ZMAX % SUB == 0, "sub-chunks of whole slice pairs");
     constexpr unsigned kElem = QUAD ? sizeof(uint2) : sizeof(float);
     const int nos = NOS > 0 ? NOS : p.nos;
     const int lane = threadIdx.x, warp = threadIdx.y;
