@@ -750,11 +750,14 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
                 "h2d_gbs": out["h2d_bytes"] / (h2d_ms * 1e-3) / 1e9,
                 "calling_thread_cpu": cpu_ms,
                 "stages_ms_per_step": e_stages,
-                "compute_stream_idle": e_ms - sum(e_stages.values()),
-                "note": "the host path streams the copy in chunks under the compute: e2e = device step + the "
-                        "first chunk's copy + what does not overlap; stages_ms_per_step are the compute "
-                        "stream's stage times in the e2e steps and compute_stream_idle the rest of the step; "
-                        "calling_thread_cpu includes the wait for the stream (a spinning synchronise)"}}
+                "backprojection_stream_idle": e_ms - e_stages.get("backproject", 0.0) - e_stages.get("finalize", 0.0),
+                "note": "the host path streams the copy in chunks under the compute, and runs the preparation "
+                        "(adaptive filter, rebin, ramp filter, edge patches) on a stream of its own beside the "
+                        "backprojections: stages_ms_per_step are each stage's event times in the e2e steps "
+                        "(the preparation's overlap the backprojections'), backprojection_stream_idle the part "
+                        "of the step in which the backprojection stream had no work (waiting for the first "
+                        "block's frames and rows, then any preparation not hidden); calling_thread_cpu includes "
+                        "the wait for the stream (a spinning synchronise)"}}
         if headline and not args.no_whole_scan:
             def ws_host_step():
                 L.call(alt_host, C.byref(mr), hp, fp, C.c_float(0.0))

@@ -99,7 +99,19 @@ struct Context {
     DeviceBuffer raw_in2;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    // streamed whole-scan path: the preparation (adaptive filter, rebin, ramp
+    // filter, edge patches) on a stream of its own, at a higher priority than
+    // the backprojections it feeds; prep_ready orders a block's backprojection
+    // after its rows, bp_done[i] a patch region's reuse after the
+    // backprojection that read it
+    cudaStream_t prep_stream = nullptr;
+    cudaEvent_t prep_ready = nullptr, bp_done[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> chunk_copied;  // whole-scan host path: one per chunk
+    // streamed whole-scan path: a block's edge-frame flags read back into
+    // pinned memory, flags_ready recorded behind the copy
+    unsigned char *flags_host = nullptr;
+    size_t flags_host_bytes = 0;
+    cudaEvent_t flags_ready = nullptr;
     // whole-scan file path: two pinned staging buffers and their reuse events
     void *stage[2] = {nullptr, nullptr};
     size_t stage_bytes = 0;
@@ -487,7 +499,19 @@ static void release_context(Context &c, bool device_sync, bool unbind)
             c.stage_free[i] = nullptr;
             c.stage[i] = nullptr;
         }
+        if (c.flags_ready) cudaEventDestroy(c.flags_ready);
+        c.flags_ready = nullptr;
         c.stage_bytes = 0;
+        if (c.flags_host) cudaFreeHost(c.flags_host);
+        c.flags_host = nullptr;
+        c.flags_host_bytes = 0;
+        if (c.prep_stream) {
+            cudaEventDestroy(c.prep_ready);
+            for (int i = 0; i < 2; ++i) cudaEventDestroy(c.bp_done[i]);
+            cudaStreamDestroy(c.prep_stream);
+            c.prep_stream = nullptr;
+            c.prep_ready = c.bp_done[0] = c.bp_done[1] = nullptr;
+        }
         cudaStreamDestroy(c.copy_stream);
         c.copy_stream = nullptr;
     }
@@ -665,6 +689,8 @@ static int drained(Context &c, Body &&body)
 {
     int st = body();
     cudaError_t e1 = c.copy_stream ? cudaStreamSynchronize(c.copy_stream) : cudaSuccess;
+    const cudaError_t e0 = c.prep_stream ? cudaStreamSynchronize(c.prep_stream) : cudaSuccess;
+    if (e1 == cudaSuccess) e1 = e0;
     cudaError_t e2 = cudaStreamSynchronize(c.stream);
     if (st == CTBB_OK && (e1 != cudaSuccess || e2 != cudaSuccess)) {
         set_error("device work of this call failed: %s",
@@ -1601,8 +1627,23 @@ static int ensure_copy_stream(Context &c)
         CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.consumed[i], cudaEventDisableTiming));
         CTBB_CUDA_TRY(cudaEventRecord(c.consumed[i], c.copy_stream));
     }
+    int least = 0, greatest = 0;
+    CTBB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CTBB_CUDA_TRY(cudaStreamCreateWithPriority(&c.prep_stream, cudaStreamNonBlocking, greatest));
+    CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.prep_ready, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.bp_done[i], cudaEventDisableTiming));
     return CTBB_OK;
 }
+
+// Enqueues on another stream of the context while in scope: the stage
+// helpers take the context's stream, and the streamed path runs its
+// preparation on c.prep_stream.  The caller holds c.mu.
+struct OnStream {
+    Context &c;
+    cudaStream_t saved;
+    OnStream(Context &cx, cudaStream_t s) : c(cx), saved(cx.stream) { c.stream = s; }
+    ~OnStream() { c.stream = saved; }
+};
 
 // Where the streamed whole-scan path gets the union window's frames: begin()
 // starts the copies of all chunks (each recording chunk_copied[k] on the copy
@@ -1671,16 +1712,37 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
     CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
+    // the union's rows, then two patch regions for the blocks' re-made edge
+    // views (block b's in region b & 1: a block's patch is written while the
+    // block before it may still be backprojecting)
+    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + 2 * max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
     CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
     if (max_patch) {
         CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
         CTBB_TRY(c.dirty.ensure(max_pull));
+        if (c.flags_host_bytes < max_pull) {
+            if (c.flags_host) cudaFreeHost(c.flags_host);
+            c.flags_host = nullptr;
+            c.flags_host_bytes = 0;
+            CTBB_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(&c.flags_host), max_pull, cudaHostAllocDefault));
+            c.flags_host_bytes = max_pull;
+        }
+        if (!c.flags_ready) CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.flags_ready, cudaEventDisableTiming));
     }
     CTBB_TRY(c.image.ensure(plane * mr->ri.n_slices_recon * sizeof(float)));
     CTBB_TRY(c.final_stack.ensure(plane * (size_t)(n_final > 0 ? n_final : 1) * sizeof(float)));
+    // Two compute streams: the preparation (adaptive filter, rebin, ramp
+    // filter, edge flags and patches) on c.prep_stream, the backprojections
+    // on the context's stream.  A block's backprojection waits for the
+    // preparation enqueued before it (its rows are final); the preparation of
+    // later chunks and blocks runs beside it, and reading a block's edge flags
+    // never waits for a backprojection.  Both start after the work already on
+    // the context's stream.
+    const cudaStream_t bp_stream = c.stream, prep = c.prep_stream;
+    CTBB_CUDA_TRY(cudaEventRecord(c.prep_ready, bp_stream));
+    CTBB_CUDA_TRY(cudaStreamWaitEvent(prep, c.prep_ready, 0));
     // the union window in chunks of whole focal-spot cycles; the copy stream
-    // starts once the compute stream has finished with the buffer
+    // starts once the compute streams have finished with the buffer
     const int n_ffs = (int)dg.n_ffs;
     int chunk = (G + scan_chunks() - 1) / scan_chunks();
     chunk = ((chunk + n_ffs - 1) / n_ffs) * n_ffs;
@@ -1690,7 +1752,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
         CTBB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         c.chunk_copied.push_back(e);
     }
-    CTBB_CUDA_TRY(cudaEventRecord(c.consumed[0], c.stream));
+    CTBB_CUDA_TRY(cudaEventRecord(c.consumed[0], prep));
     CTBB_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.consumed[0], 0));
     float *d_raw = c.raw_in.as<float>();
     int status = feed.begin(c, g0, g1, chunk, n_chunks, d_raw);
@@ -1698,7 +1760,7 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     RebinTables rt;
     if (status == CTBB_OK) status = build_rebin_tables(mg, &rt);
     rt.split_view_coord = 1;  // the union's frame offsets are large
-    if (status == CTBB_OK) status = upload_rebin_tables(rt, &c.rebin_tables, c.stream);
+    if (status == CTBB_OK) status = upload_rebin_tables(rt, &c.rebin_tables, prep);
     AfStream af(mg);
     const int V = (int)dg.n_views;
     int v_done = 0;
@@ -1706,34 +1768,37 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     for (int k = 0; k < n_chunks && status == CTBB_OK; ++k) {
         status = feed.issued(k);
         if (status != CTBB_OK) break;
-        status = cudaStreamWaitEvent(c.stream, c.chunk_copied[k], 0) == cudaSuccess ? CTBB_OK : CTBB_ERR_CUDA;
+        status = cudaStreamWaitEvent(prep, c.chunk_copied[k], 0) == cudaSuccess ? CTBB_OK : CTBB_ERR_CUDA;
         if (status != CTBB_OK) {
             set_error("scan: cudaStreamWaitEvent failed");
             break;
         }
         int arrived = std::min(G, (k + 1) * chunk);
         {
-            StageScope scope(c, 0);
-            status = af.advance(mg, d_raw, c.raw_filt.as<float>(), c.scratch.as<float>(), arrived, c.stream);
-        }
-        if (status != CTBB_OK) break;
-        // views whose frames are all final
-        int v_ready = V;
-        if (af.filtered() < G) {
-            v_ready = 0;
-            while (v_ready < V && rebin_frames_needed(rt, v_ready) <= af.filtered()) ++v_ready;
-        }
-        if (v_ready > v_done) {
+            OnStream on(c, prep);
             {
-                StageScope scope(c, 1);
-                status = launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream,
-                                      v_done, v_ready);
+                StageScope scope(c, 0);
+                status = af.advance(mg, d_raw, c.raw_filt.as<float>(), c.scratch.as<float>(), arrived, c.stream);
             }
             if (status != CTBB_OK) break;
-            status = filter_scan_rows(c, (size_t)v_done * dg.n_rows, (size_t)(v_ready - v_done) * dg.n_rows,
-                                      (int)dg.n_rows, (int)dg.n_os);
-            if (status != CTBB_OK) break;
-            v_done = v_ready;
+            // views whose frames are all final
+            int v_ready = V;
+            if (af.filtered() < G) {
+                v_ready = 0;
+                while (v_ready < V && rebin_frames_needed(rt, v_ready) <= af.filtered()) ++v_ready;
+            }
+            if (v_ready > v_done) {
+                {
+                    StageScope scope(c, 1);
+                    status = launch_rebin(rt, c.rebin_tables, c.raw_filt.as<float>(), c.rebin.as<float>(), c.stream,
+                                          v_done, v_ready);
+                }
+                if (status != CTBB_OK) break;
+                status = filter_scan_rows(c, (size_t)v_done * dg.n_rows, (size_t)(v_ready - v_done) * dg.n_rows,
+                                          (int)dg.n_rows, (int)dg.n_os);
+                if (status != CTBB_OK) break;
+                v_done = v_ready;
+            }
         }
         // blocks whose views (i + k n_half, k < nht) are all ready, and, for a
         // block with edge views, whose whole window has arrived
@@ -1751,30 +1816,47 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             mr->ri = blocks[b_done];
             ViewRows vr;
             vr.off = union_view_offset(blocks[b_done], g0);
-            vr.patch = dg.n_views;
+            vr.patch = dg.n_views + (b_done & 1) * max_patch;
             if (e.any()) {
+                OnStream on(c, prep);
                 float *d_block_scratch = c.scratch.as<float>() + af_union;
                 status = edge_dirty_frames(c, mb, e, d_raw, c.scratch.as<float>(),
                                            c.scratch.as<float>() + 5 * (size_t)dg.n_proj_pull, g0, g1,
                                            d_block_scratch, c.dirty.as<unsigned char>());
-                std::vector<unsigned char> dirty(db.n_proj_pull);
                 if (status == CTBB_OK &&
-                    (cudaMemcpyAsync(dirty.data(), c.dirty.ptr, dirty.size(), cudaMemcpyDeviceToHost, c.stream) !=
+                    (cudaMemcpyAsync(c.flags_host, c.dirty.ptr, db.n_proj_pull, cudaMemcpyDeviceToHost, prep) !=
                          cudaSuccess ||
-                     cudaStreamSynchronize(c.stream) != cudaSuccess)) {
+                     cudaEventRecord(c.flags_ready, prep) != cudaSuccess ||
+                     cudaEventSynchronize(c.flags_ready) != cudaSuccess)) {
                     set_error("whole scan: reading the edge frames' flags failed");
                     status = CTBB_ERR_CUDA;
                 }
                 if (status != CTBB_OK) break;
-                const auto runs = dirty_view_runs(e, block_rebin_tables(rt, db), dirty.data(), (int)db.n_proj_pull);
+                const auto runs = dirty_view_runs(e, block_rebin_tables(rt, db), c.flags_host, (int)db.n_proj_pull);
                 vr.slot.assign((size_t)e.n_used, -1);
                 size_t made = 0;
+                // the patch region's previous reader, block b - 2, is done
+                if (b_done >= 2 && cudaStreamWaitEvent(prep, c.bp_done[b_done & 1], 0) != cudaSuccess) {
+                    set_error("scan: cudaStreamWaitEvent failed");
+                    status = CTBB_ERR_CUDA;
+                    break;
+                }
                 status = run_edge_patch(c, mb, rt, runs, d_raw, c.scratch.as<float>(), g0, d_block_scratch,
-                                        dg.n_views, &vr, &made);
+                                        vr.patch, &vr, &made);
             }
             if (status != CTBB_OK) break;
+            if (cudaEventRecord(c.prep_ready, prep) != cudaSuccess ||
+                cudaStreamWaitEvent(bp_stream, c.prep_ready, 0) != cudaSuccess) {
+                set_error("scan: ordering the backprojection after its rows failed");
+                status = CTBB_ERR_CUDA;
+                break;
+            }
             float *slab = c.image.as<float>() + b_done * n_block * plane;
             status = backproject_scan_rows(c, *mr, slab, vr);
+            if (status == CTBB_OK && cudaEventRecord(c.bp_done[b_done & 1], bp_stream) != cudaSuccess) {
+                set_error("scan: cudaEventRecord failed");
+                status = CTBB_ERR_CUDA;
+            }
             ++b_done;
         }
     }
@@ -1785,6 +1867,8 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
         set_error("whole scan: %zu of %zu blocks left unfinished", blocks.size() - b_done, blocks.size());
         return CTBB_ERR_STATE;
     }
+    // the last backprojection waited for all the preparation: the tensor-core
+    // filter's error flag is final on the context's stream too
     CTBB_TRY(do_finalize(c, *mr, c.image.as<float>(), c.final_stack.as<float>(), mu_water));
     CTBB_CUDA_TRY(cudaMemcpyAsync(h_final, c.final_stack.ptr, plane * (size_t)n_final * sizeof(float),
                                   cudaMemcpyDeviceToHost, c.stream));
