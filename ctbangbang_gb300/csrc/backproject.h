@@ -99,7 +99,9 @@ size_t backproject_partial_bytes(const BpParams &p, const BpShape &shape);
 // Device bytes launch_backproject_batch needs for n blocks' parameters.
 size_t backproject_batch_bytes(size_t n_blocks);
 // All blocks (of any scans; one row storage and row length) in one launch of
-// the given shape; d_buf holds backproject_batch_bytes(blocks.size()).
+// the given shape -- the column form one launch per angle chunk, each adding
+// to the blocks' images in chunk order; d_buf holds
+// backproject_batch_bytes(blocks.size()).
 int launch_backproject_batch(const std::vector<BpParams> &blocks, const BpShape &shape, void *d_buf,
                              size_t buf_bytes, cudaStream_t stream);
 int launch_backproject(const struct recon_metadata &mr, const BackprojectTables &t,
