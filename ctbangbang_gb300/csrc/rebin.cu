@@ -273,8 +273,11 @@ __device__ __forceinline__ void view_taps_split(int n_ffs, int proj, float t_alp
     float cf = floorf(c);
     float c_frac = __fsub_rn(c, cf);  // exact: same binade or finer
     int J = n_ffs * proj - (int)cf;
-    int Q = J >= 0 ? J / n_ffs : -((-J + n_ffs - 1) / n_ffs);
-    int m = J - Q * n_ffs;
+    // floor(J / n_ffs) and its remainder, n_ffs a power of two (1, 2, 4): an
+    // arithmetic shift floors for negative J as well
+    const int lg = n_ffs >> 1;  // log2 n_ffs for 1, 2, 4
+    int Q = J >> lg;
+    int m = J - (Q << lg);
     float r = __fsub_rn((float)m, c_frac);  // in (-1, n_ffs)
     r = n_ffs == 1 ? r : __fmul_rn(r, n_ffs == 2 ? 0.5f : 0.25f);
     if (r < 0.0f) {  // floor
