@@ -198,7 +198,10 @@ const char *ctbb_version(void);
 int ctbb_struct_layout(size_t *out, int n);
 
 /* Stream on which all device work of the following calls is issued
-   (a cudaStream_t passed as void*; NULL = legacy default stream). */
+   (a cudaStream_t passed as void*; NULL = legacy default stream).  The
+   streamed whole-scan calls (ctbb_reconstruct_scan_host / _file) also use a
+   copy stream and a preparation stream of the library's own, ordered after
+   the work already on this stream and joined before they return. */
 int ctbb_set_stream(void *stream);
 
 /* ------------------------------------------------------------------------- */
