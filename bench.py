@@ -729,10 +729,13 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
         lib.ctbb_profile_enable(1)
         t0 = time.perf_counter()
         c0 = time.thread_time()
+        e_marks = [t0]
         for _ in range(args.steps):
-            e2e_step()
+            e2e_step()  # returns with the stack in host memory
+            e_marks.append(time.perf_counter())
         torch.cuda.synchronize()
         e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist)
+        e_steps = sorted((e_marks[k + 1] - e_marks[k]) * 1e3 for k in range(args.steps))
         cpu_ms = (time.thread_time() - c0) * 1e3 / args.steps
         lib.ctbb_profile_enable(0)
         e_stage_ms = (C.c_double * 5)()
@@ -749,6 +752,7 @@ def measure_config(args, torch, lib, config, rank, world, dist, headline):
                 "h2d_copy_alone": h2d_ms, "d2h_copy_alone": d2h_ms,
                 "h2d_gbs": out["h2d_bytes"] / (h2d_ms * 1e-3) / 1e9,
                 "calling_thread_cpu": cpu_ms,
+                "step_ms_min_median_max": [e_steps[0], e_steps[len(e_steps) // 2], e_steps[-1]],
                 "stages_ms_per_step": e_stages,
                 "backprojection_stream_idle": e_ms - e_stages.get("backproject", 0.0) - e_stages.get("finalize", 0.0),
                 "note": "the host path streams the copy in chunks under the compute, and runs the preparation "

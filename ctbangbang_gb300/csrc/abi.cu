@@ -1253,8 +1253,7 @@ static int reconstruct_scan_device_in(Context &c, struct recon_metadata *mr, con
         for (size_t b = 0; b < prep.blocks.size(); ++b) {
             mr->ri = prep.blocks[b];
             float *slab = c.image.as<float>() + b * n_block * plane;
-            const BpShape fallback =
-                fit_bp_shape(default_bp_shape(bp_zpt(), c.storage != 0), prep.tables[b].nht);
+            const BpShape fallback = window_bp_shape(bp_zpt(), c.storage != 0, prep.tables[b].nht);
             BpParams p;
             CTBB_TRY(prepared_block_params(c, *mr, prep, b, slab, fallback, &p));
             BpShape shape = fallback;
@@ -1353,7 +1352,7 @@ extern "C" int ctbb_batch_add_device(struct recon_metadata *mr, const float *d_s
         for (size_t b = 0; st == CTBB_OK && b < sl.prep.blocks.size(); ++b) {
             mr->ri = sl.prep.blocks[b];
             float *slab = c.image.as<float>() + b * mr->ri.n_slices_block * plane;
-            const BpShape fallback = fit_bp_shape(default_bp_shape(8, c.storage != 0), sl.prep.tables[b].nht);
+            const BpShape fallback = window_bp_shape(8, c.storage != 0, sl.prep.tables[b].nht);
             BpParams p;
             BpShape shape = fallback;
             st = prepared_block_params(c, *mr, sl.prep, b, slab, fallback, &p);

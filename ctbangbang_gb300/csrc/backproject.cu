@@ -24,7 +24,7 @@
 // 32 slices: per angle it computes the geometry of each half turn once and
 // parks it in shared memory, then runs the slices in sub-chunks of 8, each
 // fetching all of a visit's footprints before it uses any (one wait on the
-// gathers per visit); 128-thread CTAs of 16 x 8 columns.  The slice-chunk form
+// gathers per visit); 128-thread CTAs of 16 x 8 columns, 8 per SM.  The slice-chunk form
 // (backproject_tile; windows of more than 8 half turns) gives a thread ZPT (8)
 // consecutive slices of a column, 128-thread CTAs of 32 x 4 columns.  In both
 // each warp is an 8 x 4 tile of columns so that its gathers fall on few
@@ -1124,6 +1124,27 @@ BpShape fit_bp_shape(const BpShape &s, int nht)
     return t;
 }
 
+BpShape window_bp_shape(int zpt, bool quad, int nht)
+{
+    BpShape s = default_bp_shape(zpt, quad);
+    if (s.col && nht <= kColumnMaxHalfTurns && s.zpt == 32) {
+        // Measured per window on 256^2 and 512^2 blocks of 16-64 detector rows
+        // (FP32 rows and FP16 words alike), against 32 slices at 8 CTAs per
+        // SM: 16 slices per thread 11-13 % faster at 6-7 half turns and 2-6 %
+        // at 5; 7 CTAs per SM 0.5-1.7 % faster at 4; at 2-3 half turns 32
+        // slices at 8 CTAs are the fastest.
+        static const bool zpt_named = getenv("CTBB_BP_COL_ZPT") != nullptr;
+        static const bool minb_named = getenv("CTBB_BP_MINB") != nullptr;
+        if (nht >= 5 && !zpt_named) {
+            s.zpt = 16;
+            s.min_blocks = 8;
+        } else if (nht == 4 && !minb_named && s.min_blocks == 8) {
+            s.min_blocks = 7;
+        }
+    }
+    return fit_bp_shape(s, nht);
+}
+
 BpShape default_bp_shape(int zpt, bool quad)
 {
     if (bp_column_form()) {
@@ -1131,8 +1152,9 @@ BpShape default_bp_shape(int zpt, bool quad)
         s.col = 1;
         s.zpt = bp_column_zpt();
         s.threads = 128;
-        const int mb = bp_min_blocks();
-        s.min_blocks = (s.zpt <= 16 && mb == 8) ? 8 : (mb == 6 ? 6 : 7);
+        // 8 CTAs per SM (64 registers) unless CTBB_BP_MINB names 6 or 7
+        const int mb = getenv("CTBB_BP_MINB") ? bp_min_blocks() : 8;
+        s.min_blocks = mb == 6 ? 6 : (mb == 7 ? 7 : 8);
         // CTAs of 16 x 8 voxel columns unless CTBB_BP_CTA_W names the width
         s.cta_w = getenv("CTBB_BP_CTA_W") ? bp_cta_width() : 16;
         s.warp_w = bp_warp_width();
@@ -1153,8 +1175,8 @@ BpShape default_bp_shape(int zpt, bool quad)
     return s;
 }
 
-// The column form's instances: 128-thread CTAs; at most 32 slices per thread
-// (7 or 6 CTAs per SM) or at most 16 (8 CTAs per SM, 64 registers).
+// The column form's instances: 128-thread CTAs, at most 32 slices per thread
+// at 8 (64 registers), 7 or 6 CTAs per SM, or at most 16 slices at 8.
 // f(ZMAX, SUB, MIN_BLOCKS).
 template <class F>
 int with_column_shape(const BpShape &s, F &&f)
@@ -1167,6 +1189,8 @@ int with_column_shape(const BpShape &s, F &&f)
             return f(integral_constant<int, 32>(), integral_constant<int, 8>(), integral_constant<int, 6>());
         if (s.min_blocks == 8 && s.zpt <= 16)
             return f(integral_constant<int, 16>(), integral_constant<int, 8>(), integral_constant<int, 8>());
+        if (s.min_blocks == 8)
+            return f(integral_constant<int, 32>(), integral_constant<int, 8>(), integral_constant<int, 8>());
     }
     set_error("backproject: no column-form kernel for %d slices per thread, %d threads, %d CTAs per SM", s.zpt,
               s.threads, s.min_blocks);
@@ -1245,7 +1269,7 @@ int launch_backproject(const struct recon_metadata &mr, const BackprojectTables 
                        float *d_block, int zpt, cudaStream_t stream, const float *d_vscale, const BpShape *shape,
                        void *scratch, size_t scratch_bytes)
 {
-    const BpShape s = fit_bp_shape(shape ? *shape : default_bp_shape(zpt, d_vscale != nullptr), t.nht);
+    const BpShape s = shape ? fit_bp_shape(*shape, t.nht) : window_bp_shape(zpt, d_vscale != nullptr, t.nht);
     BpParams p;
     CTBB_TRY(make_backproject_params(mr, t, d_views, d_theta, d_zpos, d_rebin, d_block, d_vscale, s, &p));
     return launch_backproject_params(p, s, stream, scratch, scratch_bytes);
@@ -1343,10 +1367,11 @@ std::vector<BpShape> backproject_shape_candidates(bool quad)
 {
     // 128-thread CTAs are 32 x 4 (cta_w 32) or 16 x 8 (cta_w 16) voxel columns
     std::vector<BpShape> c;
+    c.push_back(BpShape{32, 128, 8, 16, 8, 1, 16});
     c.push_back(BpShape{32, 128, 7, 16, 8, 1, 16});
+    c.push_back(BpShape{32, 128, 8, 32, 8, 1, 16});
     c.push_back(BpShape{32, 128, 7, 32, 8, 1, 16});
     c.push_back(BpShape{32, 128, 7, 16, 8, 1, 8});
-    c.push_back(BpShape{16, 128, 7, 16, 8, 1, 16});
     c.push_back(BpShape{16, 128, 8, 16, 8, 1, 16});
     c.push_back(BpShape{8, 128, 7, 32, 8, 0});
     return c;

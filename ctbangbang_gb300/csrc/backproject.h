@@ -83,6 +83,10 @@ BpShape default_bp_shape(int zpt, bool quad);
 // s, or the slice-chunk form's default where s is the column form and the
 // window of nht half turns is more than it holds.
 BpShape fit_bp_shape(const BpShape &s, int nht);
+// default_bp_shape fitted to a window of nht half turns: where the knobs
+// leave them open, the column form's slices per thread and CTAs per SM
+// chosen by the window's width (measured), then fit_bp_shape.
+BpShape window_bp_shape(int zpt, bool quad, int nht);
 // Shapes the autotuner times (those the batch kernel is compiled for).
 std::vector<BpShape> backproject_shape_candidates(bool quad);
 

@@ -27,13 +27,21 @@ def torch_cuda():
 
 
 def _uneven_scans(tmp_path):
-    """Scans differing in FFS mode, rows, image size, slices and turns."""
+    """Scans differing in FFS mode, rows, image size, slices and turns: four
+    whose pull windows (17-19 half turns at 96 views per turn) only the
+    slice-chunk form holds, and three at 192 views per turn whose windows of
+    3, 6 and 7 half turns run the column form (32 slices per thread at 3, 16
+    from 5 by default; the autotuner may pick others)."""
     specs = [
         scans.tiny(0, 0, n_rows_raw=8, nx=32, ny=32, n_slices=8, seed=61, adaptive_filtration=1.0),
         scans.tiny(1, 1, n_rows_raw=4, nx=48, ny=48, n_slices=14, slice_thickness=2.5, seed=62,
                    adaptive_filtration=2.0),
         scans.tiny(0, 1, n_rows_raw=8, nx=32, ny=32, n_slices=40, seed=63, pitch=0.8),
         scans.tiny(1, 0, n_rows_raw=4, nx=64, ny=64, n_slices=6, seed=64),
+        scans.tiny(1, 1, n_rows_raw=64, n_proj_turn=192, nx=32, ny=32, n_slices=14, slice_thickness=2.5,
+                   seed=66, adaptive_filtration=2.0),
+        scans.tiny(0, 1, n_rows_raw=32, n_proj_turn=192, nx=48, ny=48, n_slices=40, seed=67, pitch=0.8),
+        scans.tiny(1, 0, n_rows_raw=16, n_proj_turn=192, nx=64, ny=64, n_slices=10, seed=68),
     ]
     return [H.Scan(sp, str(tmp_path / ("s%d" % i))) for i, sp in enumerate(specs)]
 
@@ -91,10 +99,11 @@ def test_batch_equals_each_scan_alone(torch_cuda, lib, tmp_path, storage):
 
 def test_autotuned_single_scan_path_matches_default_shape(torch_cuda, lib, tmp_path):
     """ctbb_set_autotune(1): the single-scan device path takes the tuned shape
-    per geometry class; the stack stays within the shape-rounding bar."""
+    per geometry class; the stack stays within the shape-rounding bar.  The
+    window (4 half turns at 192 views per turn) lets every candidate run."""
     torch = torch_cuda
-    scan = H.Scan(scans.tiny(1, 1, n_rows_raw=4, nx=48, ny=48, n_slices=14, slice_thickness=2.5, seed=65,
-                             adaptive_filtration=1.0), str(tmp_path))
+    scan = H.Scan(scans.tiny(1, 1, n_rows_raw=32, n_proj_turn=192, nx=48, ny=48, n_slices=14, slice_thickness=2.5,
+                             seed=65, adaptive_filtration=1.0), str(tmp_path))
     ref = _alone(torch, lib, scan)
     L.call("ctbb_set_autotune", 1)
     try:
