@@ -102,10 +102,9 @@ struct Context {
     // streamed whole-scan path: the preparation (adaptive filter, rebin, ramp
     // filter, edge patches) on a stream of its own, at a higher priority than
     // the backprojections it feeds; prep_ready orders a block's backprojection
-    // after its rows, bp_done[i] a patch region's reuse after the
-    // backprojection that read it
+    // after its rows
     cudaStream_t prep_stream = nullptr;
-    cudaEvent_t prep_ready = nullptr, bp_done[2] = {nullptr, nullptr};
+    cudaEvent_t prep_ready = nullptr;
     std::vector<cudaEvent_t> chunk_copied;  // whole-scan host path: one per chunk
     // streamed whole-scan path: a block's edge-frame flags read back into
     // pinned memory, flags_ready recorded behind the copy
@@ -507,10 +506,9 @@ static void release_context(Context &c, bool device_sync, bool unbind)
         c.flags_host_bytes = 0;
         if (c.prep_stream) {
             cudaEventDestroy(c.prep_ready);
-            for (int i = 0; i < 2; ++i) cudaEventDestroy(c.bp_done[i]);
             cudaStreamDestroy(c.prep_stream);
             c.prep_stream = nullptr;
-            c.prep_ready = c.bp_done[0] = c.bp_done[1] = nullptr;
+            c.prep_ready = nullptr;
         }
         cudaStreamDestroy(c.copy_stream);
         c.copy_stream = nullptr;
@@ -1630,7 +1628,6 @@ static int ensure_copy_stream(Context &c)
     CTBB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     CTBB_CUDA_TRY(cudaStreamCreateWithPriority(&c.prep_stream, cudaStreamNonBlocking, greatest));
     CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.prep_ready, cudaEventDisableTiming));
-    for (int i = 0; i < 2; ++i) CTBB_CUDA_TRY(cudaEventCreateWithFlags(&c.bp_done[i], cudaEventDisableTiming));
     return CTBB_OK;
 }
 
@@ -1706,15 +1703,18 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     BlockDims dg = block_dims(mg);
     const int G = (int)(g1 - g0);
     int n_final = ctbb_n_slices_final(mr);
-    size_t max_pull = 0, max_patch = 0;
-    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch);
+    size_t max_pull = 0, max_patch = 0, sum_patch = 0;
+    edge_extent(*mr, blocks, g0, g1, &max_pull, &max_patch, &sum_patch);
     const size_t af_union = adaptive_filter_scratch_floats(dg.n_proj_pull);
     CTBB_TRY(c.raw_in.ensure(dg.raw_elems() * sizeof(float)));
     CTBB_TRY(c.raw_filt.ensure(dg.raw_elems() * sizeof(float)));
-    // the union's rows, then two patch regions for the blocks' re-made edge
-    // views (block b's in region b & 1: a block's patch is written while the
-    // block before it may still be backprojecting)
-    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + 2 * max_patch) * dg.n_rows, dg.n_views * dg.n_rows));
+    // the union's rows, then a patch region per block for its re-made edge
+    // views (as the device path lays them out): the preparation never waits
+    // for a backprojection to free a region, so it runs as far ahead as the
+    // frames allow and the host enqueues every block as soon as its rows are
+    // ready
+    CTBB_TRY(prepare_scan_rows(c, mg, (dg.n_views + sum_patch) * dg.n_rows, dg.n_views * dg.n_rows));
+    size_t patch_next = dg.n_views;
     CTBB_TRY(c.scratch.ensure((af_union + adaptive_filter_scratch_floats(max_pull)) * sizeof(float)));
     if (max_patch) {
         CTBB_TRY(c.edge_raw.ensure(max_pull * dg.n_rows_raw * dg.n_channels * sizeof(float)));
@@ -1734,9 +1734,9 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
     // filter, edge flags and patches) on c.prep_stream, the backprojections
     // on the context's stream.  A block's backprojection waits for the
     // preparation enqueued before it (its rows are final); the preparation of
-    // later chunks and blocks runs beside it, and reading a block's edge flags
-    // never waits for a backprojection.  Both start after the work already on
-    // the context's stream.
+    // later chunks and blocks runs beside it, and neither reading a block's
+    // edge flags nor writing its patch waits for a backprojection.  Both
+    // start after the work already on the context's stream.
     const cudaStream_t bp_stream = c.stream, prep = c.prep_stream;
     CTBB_CUDA_TRY(cudaEventRecord(c.prep_ready, bp_stream));
     CTBB_CUDA_TRY(cudaStreamWaitEvent(prep, c.prep_ready, 0));
@@ -1815,7 +1815,8 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             mr->ri = blocks[b_done];
             ViewRows vr;
             vr.off = union_view_offset(blocks[b_done], g0);
-            vr.patch = dg.n_views + (b_done & 1) * max_patch;
+            vr.patch = patch_next;
+            patch_next += (size_t)e.n_patch();
             if (e.any()) {
                 OnStream on(c, prep);
                 float *d_block_scratch = c.scratch.as<float>() + af_union;
@@ -1834,12 +1835,6 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
                 const auto runs = dirty_view_runs(e, block_rebin_tables(rt, db), c.flags_host, (int)db.n_proj_pull);
                 vr.slot.assign((size_t)e.n_used, -1);
                 size_t made = 0;
-                // the patch region's previous reader, block b - 2, is done
-                if (b_done >= 2 && cudaStreamWaitEvent(prep, c.bp_done[b_done & 1], 0) != cudaSuccess) {
-                    set_error("scan: cudaStreamWaitEvent failed");
-                    status = CTBB_ERR_CUDA;
-                    break;
-                }
                 status = run_edge_patch(c, mb, rt, runs, d_raw, c.scratch.as<float>(), g0, d_block_scratch,
                                         vr.patch, &vr, &made);
             }
@@ -1852,10 +1847,6 @@ static int scan_streamed(Context &c, struct recon_metadata *mr, ChunkFeed &feed,
             }
             float *slab = c.image.as<float>() + b_done * n_block * plane;
             status = backproject_scan_rows(c, *mr, slab, vr);
-            if (status == CTBB_OK && cudaEventRecord(c.bp_done[b_done & 1], bp_stream) != cudaSuccess) {
-                set_error("scan: cudaEventRecord failed");
-                status = CTBB_ERR_CUDA;
-            }
             ++b_done;
         }
     }
